@@ -1,0 +1,130 @@
+"""ctypes binding of ``libpibronic_gb300.so`` (the C ABI declared in ``include/pibronic_gb300.h``).
+
+The library is loaded lazily on first use.  There is no CPU fallback: if the library is missing,
+cannot be loaded, or no CUDA device is present, every compute call raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_LOCK = threading.Lock()
+_LIB = None
+
+PBR_OK, PBR_ERR_ARG, PBR_ERR_CUDA, PBR_ERR_UNSUPPORTED, PBR_ERR_NONFINITE = 0, 1, 2, 3, 4
+_STATUS_TEXT = {
+    PBR_ERR_ARG: "invalid argument",
+    PBR_ERR_CUDA: "CUDA error",
+    PBR_ERR_UNSUPPORTED: "unsupported sizes for the compiled kernels",
+    PBR_ERR_NONFINITE: "non-finite result",
+}
+
+#: every symbol declared in include/pibronic_gb300.h
+EXPORTED = (
+    "pbr_sample_eval", "pbr_sample_q", "pbr_eval_q", "pbr_eval_q_f32",
+    "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_divide_o_matrix", "pbr_denominator",
+    "pbr_coupling_eigh", "pbr_numerator",
+    "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_version",
+)
+
+
+class PbrModel(C.Structure):
+    """Mirror of ``pbr_model``."""
+    _fields_ = [
+        ("A", C.c_int32), ("A_rho", C.c_int32), ("n_fill_rho", C.c_int32), ("N", C.c_int32),
+        ("P", C.c_int32), ("K", C.c_int32), ("precision", C.c_int32), ("pad0", C.c_int32),
+        ("tau", C.c_double), ("delta_beta", C.c_double), ("log_c0", C.c_double),
+        ("vib_cs", C.c_void_p), ("vib_th", C.c_void_p), ("vib_c", C.c_void_p),
+        ("vib_d", C.c_void_p), ("vib_e", C.c_void_p), ("vib_l", C.c_void_p),
+        ("vib_qq", C.c_void_p), ("rho_cs", C.c_void_p), ("rho_th", C.c_void_p),
+        ("rho_c", C.c_void_p), ("rho_d", C.c_void_p), ("mode_std", C.c_void_p),
+        ("src_cdf", C.c_void_p),
+    ]
+
+
+class PbrOutputs(C.Structure):
+    """Mirror of ``pbr_outputs``."""
+    _fields_ = [
+        ("s_rho", C.c_void_p), ("s_g", C.c_void_p), ("s_gp", C.c_void_p), ("s_gm", C.c_void_p),
+        ("g_coef", C.c_void_p), ("log_scale", C.c_void_p), ("q_out", C.c_void_p),
+        ("src_out", C.c_void_p), ("status", C.c_void_p),
+    ]
+
+
+def lib_path():
+    here = os.path.dirname(os.path.abspath(__file__))
+    return os.path.join(here, "_lib", "libpibronic_gb300.so")
+
+
+def _declare(lib):
+    vp, i32, i64, u64, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double
+    sig = {
+        "pbr_sample_eval": (C.c_int, [C.POINTER(PbrModel), u64, u64, i64, C.POINTER(PbrOutputs), vp]),
+        "pbr_sample_q": (C.c_int, [C.POINTER(PbrModel), u64, u64, i64, vp, vp, vp]),
+        "pbr_eval_q": (C.c_int, [C.POINTER(PbrModel), vp, i64, C.POINTER(PbrOutputs), vp]),
+        "pbr_eval_q_f32": (C.c_int, [C.POINTER(PbrModel), vp, i64, C.POINTER(PbrOutputs), vp]),
+        "pbr_o_matrix": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),
+        "pbr_scale_o_matrices": (C.c_int, [vp, i32, vp, i32, i64, i32, vp, vp]),
+        "pbr_divide_o_matrix": (C.c_int, [vp, i32, i64, i32, vp, vp]),
+        "pbr_denominator": (C.c_int, [vp, i64, i32, i32, vp, vp]),
+        "pbr_coupling_eigh": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "pbr_numerator": (C.c_int, [vp, vp, vp, i64, i32, i32, f64, vp, vp, vp]),
+        "pbr_reduce_terms": (C.c_int, [vp, vp, vp, vp, i64, f64, vp, vp, vp]),
+        "pbr_reduce_jackknife": (C.c_int, [vp, vp, vp, vp, i64, f64, f64, vp, vp, vp, vp]),
+        "pbr_reduce_blocks": (i64, [i64]),
+        "pbr_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def load(path=None):
+    """Load (once) and return the ctypes library handle; raises RuntimeError when unavailable."""
+    global _LIB
+    with _LOCK:
+        if _LIB is not None:
+            return _LIB
+        path = path or lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(
+                f"pibronic_gb300 CUDA library not built ({path}); run pibronic_gb300.build.build()")
+        lib = C.CDLL(path)
+        missing = [s for s in EXPORTED if not hasattr(lib, s)]
+        if missing:
+            raise RuntimeError(f"{path} lacks symbols {missing}")
+        _declare(lib)
+        _LIB = lib
+        return lib
+
+
+def check(status, what):
+    """Map a non-zero status to the reference's exception types (AssertionError for argument
+    and shape problems, RuntimeError for device failures)."""
+    if status == PBR_OK:
+        return
+    text = _STATUS_TEXT.get(status, f"status {status}")
+    if status in (PBR_ERR_ARG, PBR_ERR_UNSUPPORTED):
+        raise AssertionError(f"{what}: {text}")
+    raise RuntimeError(f"{what}: {text}")
+
+
+def require_cuda():
+    """The product path runs on the GPU only; fail loudly otherwise."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("pibronic_gb300 needs a CUDA device: there is no CPU fallback")
+    return torch
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor, or None."""
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def stream_handle(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)

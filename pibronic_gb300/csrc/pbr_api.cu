@@ -1,0 +1,139 @@
+// pbr_api.cu -- extern "C" entry points of the fused path (declared in include/pibronic_gb300.h).
+#include <algorithm>
+#include <cstring>
+
+#include "pbr_fused.cuh"
+
+namespace pbr {
+template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
+}
+
+namespace {
+
+int pow2ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+int ilog2(int x) {
+    int l = 0;
+    while ((1 << l) < x) ++l;
+    return l;
+}
+
+int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, uint64_t seed,
+              uint64_t offset, const pbr_outputs* out, void* stream) {
+    using namespace pbr;
+    if (!model || !out || X < 0) return PBR_ERR_ARG;
+    if (X == 0) return PBR_OK;
+    const pbr_model& m = *model;
+    if (m.A < 1 || m.A > 4) return PBR_ERR_UNSUPPORTED;
+    if (m.A_rho < m.A || m.A_rho > PBR_MAX_A_RHO) return PBR_ERR_ARG;
+    if (m.n_fill_rho != m.A) return PBR_ERR_ARG;
+    if (m.N < 1 || m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P) return PBR_ERR_ARG;
+    if (m.K != 0 && m.K != 4) return PBR_ERR_UNSUPPORTED;
+    if (m.precision != 32 && m.precision != 64) return PBR_ERR_ARG;
+    if (!out->s_rho || !out->s_g) return PBR_ERR_ARG;
+    if (m.K > 0 && (!out->s_gp || !out->s_gm)) return PBR_ERR_ARG;
+    if (!m.vib_cs || !m.vib_th || !m.vib_c || !m.vib_d || !m.vib_e || !m.vib_l || !m.vib_qq ||
+        !m.rho_cs || !m.rho_th || !m.rho_c || !m.rho_d)
+        return PBR_ERR_ARG;
+    if (qmode == kSample && (!m.mode_std || !m.src_cdf)) return PBR_ERR_ARG;
+    if (qmode != kSample && !q_in) return PBR_ERR_ARG;
+
+    FusedArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.m = m;
+    a.q_in = q_in;
+    a.X = X;
+    a.out = *out;
+    a.key0 = static_cast<uint32_t>(seed);
+    a.key1 = static_cast<uint32_t>(seed >> 32);
+    a.offset = offset;
+    a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
+    a.logG = ilog2(a.G);
+    a.C = (m.P + a.G - 1) / a.G;
+    if (qmode == kSample && a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;   // P > 256
+    a.S = kThreads / a.G;
+    const int A2 = npair(m.A);
+    a.a2p = (A2 + 3) / 4 * 4;
+    a.qstride = m.N * m.P + 1;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    switch (m.A) {
+        case 1: return launch_fused<1>(m.K, qmode, m.precision, a, st);
+        case 2: return launch_fused<2>(m.K, qmode, m.precision, a, st);
+        case 3: return launch_fused<3>(m.K, qmode, m.precision, a, st);
+        case 4: return launch_fused<4>(m.K, qmode, m.precision, a, st);
+        default: return PBR_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbr_sample_eval(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X,
+                    const pbr_outputs* out, void* stream) {
+    return run_fused(model, pbr::kSample, nullptr, X, seed, offset, out, stream);
+}
+
+int pbr_eval_q(const pbr_model* model, const double* q, int64_t X, const pbr_outputs* out,
+               void* stream) {
+    return run_fused(model, pbr::kQ64, q, X, 0, 0, out, stream);
+}
+
+int pbr_eval_q_f32(const pbr_model* model, const float* q, int64_t X, const pbr_outputs* out,
+                   void* stream) {
+    if (model && model->precision != 32) return PBR_ERR_ARG;
+    return run_fused(model, pbr::kQ32, q, X, 0, 0, out, stream);
+}
+
+int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X,
+                 float* q_out, int32_t* src_out, void* stream) {
+    using namespace pbr;
+    if (!model || !q_out || X < 0) return PBR_ERR_ARG;
+    if (X == 0) return PBR_OK;
+    const pbr_model& m = *model;
+    if (m.N < 1 || m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P) return PBR_ERR_ARG;
+    if (m.A_rho < 1 || m.A_rho > PBR_MAX_A_RHO || !m.mode_std || !m.src_cdf || !m.rho_d) return PBR_ERR_ARG;
+    if (m.precision != 32 && m.precision != 64) return PBR_ERR_ARG;
+    FusedArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.m = m;
+    a.X = X;
+    a.out.q_out = q_out;
+    a.out.src_out = src_out;
+    a.key0 = static_cast<uint32_t>(seed);
+    a.key1 = static_cast<uint32_t>(seed >> 32);
+    a.offset = offset;
+    a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
+    a.logG = ilog2(a.G);
+    a.C = (m.P + a.G - 1) / a.G;
+    if (a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;
+    a.S = kThreads / a.G;
+    a.qstride = m.N * m.P + 1;
+    const size_t esz = m.precision == 32 ? sizeof(float) : sizeof(double);
+    const int bytes = static_cast<int>((align_up(2 * m.P, 4) + a.S * a.qstride) * esz);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    auto go = [&](auto kern) -> int {
+        if (bytes > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+            return PBR_ERR_UNSUPPORTED;
+        int dev = 0, sms = 0, occ = 0;
+        PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
+        PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, bytes));
+        if (occ < 1) return PBR_ERR_UNSUPPORTED;
+        const int64_t need = (X + a.S - 1) / a.S;
+        const int grid = static_cast<int>(std::min<int64_t>(need, static_cast<int64_t>(occ) * sms));
+        kern<<<grid, kThreads, bytes, st>>>(a);
+        return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+    };
+    if (m.precision == 32) return go(sample_q_kernel<float>);
+    return go(sample_q_kernel<double>);
+}
+
+const char* pbr_version(void) { return "pibronic_gb300 0.1 sm_103a"; }
+
+}  // extern "C"

@@ -1,0 +1,6 @@
+// Fused kernel instantiations for A = 1 surfaces.
+#include "pbr_fused_launch.cuh"
+
+namespace pbr {
+template int launch_fused<1>(int, int, int, const FusedArgs&, cudaStream_t);
+}  // namespace pbr

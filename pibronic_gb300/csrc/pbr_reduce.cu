@@ -1,0 +1,184 @@
+// pbr_reduce.cu -- FP64 device reductions of the per-sample outputs into estimator moments.
+//
+// Each thread keeps Welford (count, mean, M2) triples over a strided range; triples are merged
+// with Chan's pairwise formula, first across the warp by shuffles, then across the block in
+// shared memory, then across blocks by a single-block second pass, always in the same order,
+// so results are bitwise reproducible for a given X.
+#include "pbr_common.cuh"
+
+namespace {
+
+constexpr int kRedThreads = 256;
+constexpr int64_t kPerBlock = 4096;
+constexpr int kMaxBlocks = 4096;
+
+struct Moments { double n, mean, m2; };
+
+__device__ __forceinline__ void push(Moments& s, double x) {
+    s.n += 1.0;
+    const double d = x - s.mean;
+    s.mean += d / s.n;
+    s.m2 += d * (x - s.mean);
+}
+
+__device__ __forceinline__ Moments merge(const Moments& a, const Moments& b) {
+    if (a.n == 0.0) return b;
+    if (b.n == 0.0) return a;
+    Moments r;
+    r.n = a.n + b.n;
+    const double d = b.mean - a.mean;
+    r.mean = a.mean + d * (b.n / r.n);
+    r.m2 = a.m2 + b.m2 + d * d * (a.n * b.n / r.n);
+    return r;
+}
+
+__device__ __forceinline__ Moments shfl_down(const Moments& m, int off) {
+    return Moments{__shfl_down_sync(0xffffffffu, m.n, off), __shfl_down_sync(0xffffffffu, m.mean, off),
+                   __shfl_down_sync(0xffffffffu, m.m2, off)};
+}
+
+// block-wide merge of V moment triples; result valid in thread 0
+template <int V>
+__device__ void block_merge(Moments (&m)[V]) {
+    __shared__ Moments sm[kRedThreads / 32][V];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const Moments o = shfl_down(m[v], off);
+            m[v] = merge(m[v], o);
+        }
+    if (lane == 0)
+#pragma unroll
+        for (int v = 0; v < V; ++v) sm[warp][v] = m[v];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            Moments acc = sm[0][v];
+            for (int w = 1; w < kRedThreads / 32; ++w) acc = merge(acc, sm[w][v]);
+            m[v] = acc;
+        }
+    }
+}
+
+__device__ __forceinline__ void terms(const double* rho, const double* g, const double* gp,
+                                      const double* gm, int64_t i, double db, double& r,
+                                      double& s1, double& s2) {
+    const double rh = rho[i], gg = g[i];
+    r = gg / rh;                                             // stats.py:42
+    if (gp) {
+        const double p = gp[i], m = gm[i];
+        s1 = (p - m) / rh / (2.0 * db);                      // stats.py:44-45
+        s2 = (p - 2.0 * gg + m) / rh / (db * db);            // stats.py:47-48
+    } else {
+        s1 = 0.0;
+        s2 = 0.0;
+    }
+}
+
+__global__ void terms_partial(const double* rho, const double* g, const double* gp, const double* gm,
+                              int64_t X, double db, double* scratch) {
+    Moments m[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < X;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        double r, s1, s2;
+        terms(rho, g, gp, gm, i, db, r, s1, s2);
+        push(m[0], r);
+        push(m[1], s1);
+        push(m[2], s2);
+    }
+    block_merge<3>(m);
+    if (threadIdx.x == 0)
+        for (int v = 0; v < 3; ++v) {
+            double* o = scratch + (static_cast<int64_t>(blockIdx.x) * 3 + v) * 3;
+            o[0] = m[v].n; o[1] = m[v].mean; o[2] = m[v].m2;
+        }
+}
+
+__global__ void jackknife_partial(const double* rho, const double* g, const double* gp,
+                                  const double* gm, int64_t X, double db, double kT2,
+                                  const double* totals, double* scratch) {
+    const double Sr = totals[0], S1 = totals[1], S2 = totals[2];
+    const double E0 = -S1 / Sr;
+    Moments m[2] = {{0, 0, 0}, {0, 0, 0}};
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < X;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        double r, s1, s2;
+        terms(rho, g, gp, gm, i, db, r, s1, s2);
+        const double den = Sr * (Sr - r);
+        const double dE = -(Sr * s1 - S1 * r) / den;          // f_E,i - E0
+        const double dC = ((Sr * s2 - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2;
+        push(m[0], dE);
+        push(m[1], dC);
+    }
+    block_merge<2>(m);
+    if (threadIdx.x == 0)
+        for (int v = 0; v < 2; ++v) {
+            double* o = scratch + (static_cast<int64_t>(blockIdx.x) * 2 + v) * 3;
+            o[0] = m[v].n; o[1] = m[v].mean; o[2] = m[v].m2;
+        }
+}
+
+template <int V>
+__global__ void final_merge(const double* scratch, int nblocks, double* out) {
+    Moments m[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) m[v] = Moments{0, 0, 0};
+    // each thread merges a contiguous run of partials, then the block merges threads in order
+    const int per = (nblocks + kRedThreads - 1) / kRedThreads;
+    const int b0 = threadIdx.x * per, b1 = min(nblocks, b0 + per);
+    for (int b = b0; b < b1; ++b)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const double* s = scratch + (static_cast<int64_t>(b) * V + v) * 3;
+            m[v] = merge(m[v], Moments{s[0], s[1], s[2]});
+        }
+    // ordered merge: lanes hold consecutive runs, shuffle-down merges keep the order
+    block_merge<V>(m);
+    if (threadIdx.x == 0) {
+        out[0] = m[0].n;
+#pragma unroll
+        for (int v = 0; v < V; ++v) { out[1 + 2 * v] = m[v].mean; out[2 + 2 * v] = m[v].m2; }
+    }
+}
+
+int nblocks_for(int64_t X) {
+    int64_t nb = (X + kPerBlock - 1) / kPerBlock;
+    if (nb < 1) nb = 1;
+    if (nb > kMaxBlocks) nb = kMaxBlocks;
+    return static_cast<int>(nb);
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t pbr_reduce_blocks(int64_t X) { return nblocks_for(X); }
+
+int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
+                     const double* s_gm, int64_t X, double delta_beta, double* scratch,
+                     double* moments, void* stream) {
+    if (!s_rho || !s_g || !scratch || !moments || X < 1) return PBR_ERR_ARG;
+    if ((s_gp == nullptr) != (s_gm == nullptr)) return PBR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = nblocks_for(X);
+    terms_partial<<<nb, kRedThreads, 0, st>>>(s_rho, s_g, s_gp, s_gm, X, delta_beta, scratch);
+    final_merge<3><<<1, kRedThreads, 0, st>>>(scratch, nb, moments);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s_gp,
+                         const double* s_gm, int64_t X, double delta_beta, double kB_T2,
+                         const double* totals, double* scratch, double* out, void* stream) {
+    if (!s_rho || !s_g || !s_gp || !s_gm || !totals || !scratch || !out || X < 2) return PBR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = nblocks_for(X);
+    jackknife_partial<<<nb, kRedThreads, 0, st>>>(s_rho, s_g, s_gp, s_gm, X, delta_beta, kB_T2,
+                                                  totals, scratch);
+    final_merge<2><<<1, kRedThreads, 0, st>>>(scratch, nb, out);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+}  // extern "C"

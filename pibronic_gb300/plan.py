@@ -1,0 +1,237 @@
+"""Host FP64 precompute of the model constants and their device tables (the pbr_model struct).
+
+This is the work of BoxData.preprocess / ModelVibronic(PM).precompute / ModelSampling.precompute
+(pimc.py:59-89, 172-424, 647-738), restated for the fused kernel:
+
+* The O-matrix exponent is carried as a truncated Taylor series in the beta step h,
+  phi_pa(beta + h) = sum_k phi_pa,k h^k (order K = 4 on the plus/minus path), so g(beta +- db)
+  (pimc.py:1442-1449) come out of one ring product as sum_k Tr N_k (+-db)^k.  Only the harmonic
+  O matrices depend on h; M always uses the central tau, as in the reference.
+* The coefficients of csch(w (beta+h)/P), tanh(w (beta+h)/(2P)) and ln prefactor(beta+h) are
+  built here with truncated-power-series arithmetic in FP64.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .constants import beta as beta_of
+
+F64 = np.float64
+
+
+# ---------------------------------------------------------------------------------------------
+# truncated power series (coefficient arrays along the last axis)
+# ---------------------------------------------------------------------------------------------
+def tps_sinh_cosh(x0, slope, K):
+    """Series of sinh and cosh of x0 + slope*h: d^k/dh^k alternates between sinh and cosh."""
+    x0 = np.asarray(x0, dtype=F64)
+    slope = np.asarray(slope, dtype=F64)
+    sh, ch = np.sinh(x0), np.cosh(x0)
+    S = np.empty(x0.shape + (K + 1,))
+    Cc = np.empty(x0.shape + (K + 1,))
+    for k in range(K + 1):
+        f = slope ** k / math.factorial(k)
+        S[..., k] = f * (sh if k % 2 == 0 else ch)
+        Cc[..., k] = f * (ch if k % 2 == 0 else sh)
+    return S, Cc
+
+
+def tps_recip(a):
+    K = a.shape[-1] - 1
+    r = np.zeros_like(a)
+    r[..., 0] = 1.0 / a[..., 0]
+    for k in range(1, K + 1):
+        acc = np.zeros(a.shape[:-1])
+        for i in range(1, k + 1):
+            acc += a[..., i] * r[..., k - i]
+        r[..., k] = -acc / a[..., 0]
+    return r
+
+
+def tps_mul(a, b):
+    K = a.shape[-1] - 1
+    c = np.zeros(np.broadcast(a[..., 0], b[..., 0]).shape + (K + 1,))
+    for k in range(K + 1):
+        for i in range(k + 1):
+            c[..., k] += a[..., i] * b[..., k - i]
+    return c
+
+
+def tps_log(a):
+    K = a.shape[-1] - 1
+    lg = np.zeros_like(a)
+    lg[..., 0] = np.log(a[..., 0])
+    for k in range(1, K + 1):
+        acc = a[..., k] * k
+        for i in range(1, k):
+            acc = acc - i * lg[..., i] * a[..., k - i]
+        lg[..., k] = acc / (k * a[..., 0])
+    return lg
+
+
+def harmonic_series(omega, beta, P, K):
+    """Taylor coefficients in h of csch(w(beta+h)/P), tanh(w(beta+h)/(2P)) and ln sinh(w(beta+h)/P).
+    Shapes (N, K+1)."""
+    omega = np.asarray(omega, dtype=F64)
+    s1, c1 = tps_sinh_cosh(omega * beta / P, omega / P, K)
+    s2, c2 = tps_sinh_cosh(omega * beta / (2 * P), omega / (2 * P), K)
+    return tps_recip(s1), tps_mul(s2, tps_recip(c2)), tps_log(s1)
+
+
+def prefactor_log_series(tilde_energy, omega, beta, P, K):
+    """ln[exp(-tau Etilde_a) prod_j csch(tau w_j)^(1/2)] at tau = (beta+h)/P, shape (A, K+1)
+    (pimc.py:74-81)."""
+    _, _, lsinh = harmonic_series(omega, beta, P, K)
+    out = np.zeros((len(tilde_energy), K + 1))
+    out[:, 0] = -beta / P * tilde_energy
+    if K >= 1:
+        out[:, 1] = -tilde_energy / P
+    out -= 0.5 * lsinh.sum(axis=0)[None, :]
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# ring normal modes
+# ---------------------------------------------------------------------------------------------
+def ring_mode_eigenvalues(P):
+    """Eigenvalues of the ring adjacency C (circulant [0,1,0..0,1], pimc.py:684-689) in the real
+    Fourier order the sampler uses: slot 0 constant, slots 2k-1, 2k the cos/sin pair of
+    frequency k, slot P-1 the alternating mode when P is even."""
+    lam = np.empty(P)
+    lam[0] = 2.0
+    for k in range(1, (P - 1) // 2 + 1):
+        lam[2 * k - 1] = lam[2 * k] = 2.0 * math.cos(2.0 * math.pi * k / P)
+    if P % 2 == 0:
+        lam[P - 1] = -2.0
+    return lam
+
+
+def ring_mode_basis(P):
+    """The orthonormal basis B[p, s] matching ring_mode_eigenvalues (q_p = sum_s B_ps cc_s)."""
+    p = np.arange(P)
+    B = np.empty((P, P))
+    B[:, 0] = 1.0 / math.sqrt(P)
+    for k in range(1, (P - 1) // 2 + 1):
+        B[:, 2 * k - 1] = math.sqrt(2.0 / P) * np.cos(2 * math.pi * k * p / P)
+        B[:, 2 * k] = math.sqrt(2.0 / P) * np.sin(2 * math.pi * k * p / P)
+    if P % 2 == 0:
+        B[:, P - 1] = (-1.0) ** p / math.sqrt(P)
+    return B
+
+
+def pair_index(b, c):
+    return b * (b + 1) // 2 + c
+
+
+# ---------------------------------------------------------------------------------------------
+# prepared models
+# ---------------------------------------------------------------------------------------------
+class PreparedModels:
+    """Everything the device tables are built from (FP64, host)."""
+
+    def __init__(self, vib, rho, P, temperature=None, beta=None, delta_beta=None, K=None):
+        from .vibronic_io import VMK
+        self.beta = beta if beta is not None else beta_of(temperature)
+        self.P = P
+        self.tau = self.beta / P
+        self.delta_beta = 0.0 if delta_beta is None else float(delta_beta)
+        self.K = (4 if delta_beta is not None else 0) if K is None else K
+        A, N = int(vib[VMK.A]), int(vib[VMK.N])
+        Ar = int(rho[VMK.A])
+        assert int(rho[VMK.N]) == N, "sampling and coupled models must have the same modes"
+        self.A, self.N, self.A_rho = A, N, Ar
+        assert P >= 3, "circulant matrix requires 3 or more beads"
+        # reference fills min(A, A_rho) rho surfaces and fails when A_rho < A (pimc.py:1110)
+        assert Ar >= A, "the sampling model needs at least as many surfaces as the coupled model"
+        self.n_fill_rho = A
+        w = np.asarray(vib[VMK.w], dtype=F64)
+        E = np.array(vib[VMK.E], dtype=F64)
+        L = np.array(vib[VMK.G1], dtype=F64)
+        Q = np.array(vib[VMK.G2], dtype=F64)
+        lin_diag = np.array([L[:, a, a] for a in range(A)])              # (A,N)
+        self.vib_delta = -0.5 * (lin_diag ** 2 / w[None, :]).sum(axis=1)  # pimc.py:176
+        self.vib_tilde = np.diag(E) + self.vib_delta                      # pimc.py:75-76
+        self.vib_shift = -lin_diag / w[None, :]                            # pimc.py:212
+        for a in range(A):                                                 # pimc.py:214-217
+            L[:, a, a] = 0.0
+            E[a, a] = 0.0
+        # V(q) must be symmetric in the surfaces (pimc.py:1169)
+        assert np.allclose(E, E.T) and np.allclose(L, L.transpose(0, 2, 1)) \
+            and np.allclose(Q, Q.transpose(0, 1, 3, 2)), "coupling terms are not symmetric in surfaces"
+        self.vib_omega, self.vib_E, self.vib_L, self.vib_Q = w, E, L, Q
+        wr = np.asarray(rho[VMK.w], dtype=F64)
+        Lr = np.asarray(rho[VMK.G1], dtype=F64)                            # (N, A_rho)
+        self.rho_delta = -0.5 * (Lr ** 2 / wr[:, None]).sum(axis=0)       # pimc.py:338
+        Er = np.asarray(rho[VMK.E], dtype=F64)
+        weight = np.exp(-self.beta * (Er + self.rho_delta))               # pimc.py:343
+        weight /= np.prod(np.sinh(self.beta * wr / 2.0))                  # pimc.py:347
+        self.state_weight = weight / weight.sum()                         # pimc.py:350
+        self.rho_tilde = Er + self.rho_delta
+        self.rho_shift = (-Lr / wr[:, None]).T.copy()                     # pimc.py:376
+        self.rho_omega = wr
+
+    # -- host constants ----------------------------------------------------------------------
+    def tables(self):
+        """FP64 numpy tables keyed like the pbr_model fields, plus log_c0."""
+        A, N, P, K, Ar = self.A, self.N, self.P, self.K, self.A_rho
+        csch_s, tanh_s, _ = harmonic_series(self.vib_omega, self.beta, P, K)
+        vib_c = prefactor_log_series(self.vib_tilde, self.vib_omega, self.beta, P, K)  # (A,K+1)
+        rcsch, rtanh, _ = harmonic_series(self.rho_omega, self.beta, P, 0)
+        rho_c = prefactor_log_series(self.rho_tilde, self.rho_omega, self.beta, P, 0)[:, 0]
+        log_c0 = float(max(vib_c[:, 0].max(), rho_c[:A].max()))
+        vib_c[:, 0] -= log_c0
+        rho_c = rho_c - log_c0
+        A2, N2 = A * (A + 1) // 2, N * (N + 1) // 2
+        e = np.array([self.vib_E[b, c] for b in range(A) for c in range(b + 1)])
+        lt = np.array([[self.vib_L[j, b, c] for b in range(A) for c in range(b + 1)] for j in range(N)])
+        Q = self.vib_Q
+        qq = np.empty((N2, A2))
+        for d in range(N):
+            for e_ in range(d + 1):
+                row = pair_index(d, e_)
+                for b in range(A):
+                    for c in range(b + 1):
+                        if d == e_:
+                            qq[row, pair_index(b, c)] = 0.5 * Q[d, d, b, c]
+                        else:
+                            qq[row, pair_index(b, c)] = 0.5 * (Q[d, e_, b, c] + Q[e_, d, b, c])
+        lam = ring_mode_eigenvalues(P)
+        coth_r = 1.0 / np.tanh(self.tau * self.rho_omega)
+        csch_r = 1.0 / np.sinh(self.tau * self.rho_omega)
+        invcov = 2.0 * coth_r[None, :, None] - csch_r[None, :, None] * lam[None, None, :]  # pimc.py:402
+        mode_std = np.broadcast_to(np.sqrt(1.0 / invcov), (Ar, N, P)).copy()
+        return {
+            "vib_cs": 0.5 * csch_s.T.copy(), "vib_th": 0.5 * tanh_s.T.copy(), "vib_c": vib_c.T.copy(),
+            "vib_d": self.vib_shift.copy(), "vib_e": e, "vib_l": lt.reshape(N, A2), "vib_qq": qq,
+            "rho_cs": 0.5 * rcsch[:, 0], "rho_th": 0.5 * rtanh[:, 0], "rho_c": rho_c,
+            "rho_d": self.rho_shift.copy(), "mode_std": mode_std,
+            "src_cdf": np.cumsum(self.state_weight), "log_c0": log_c0,
+        }
+
+
+class DevicePlan:
+    """The device-resident tables of one PreparedModels and the pbr_model struct pointing at them."""
+
+    FIELDS = ("vib_cs", "vib_th", "vib_c", "vib_d", "vib_e", "vib_l", "vib_qq", "rho_cs", "rho_th",
+              "rho_c", "rho_d", "mode_std", "src_cdf")
+
+    def __init__(self, prep, precision=32, device=None):
+        from . import _native
+        torch = _native.require_cuda()
+        assert precision in (32, 64)
+        self.prep, self.precision = prep, precision
+        tabs = prep.tables()
+        dt = torch.float32 if precision == 32 else torch.float64
+        dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.tensors = {k: torch.as_tensor(np.ascontiguousarray(tabs[k]).ravel(), dtype=dt).to(dev)
+                        for k in self.FIELDS}
+        m = _native.PbrModel()
+        m.A, m.A_rho, m.n_fill_rho, m.N, m.P, m.K = prep.A, prep.A_rho, prep.n_fill_rho, prep.N, prep.P, prep.K
+        m.precision = precision
+        m.tau, m.delta_beta, m.log_c0 = prep.tau, prep.delta_beta, tabs["log_c0"]
+        for k in self.FIELDS:
+            setattr(m, k, self.tensors[k].data_ptr())
+        self.struct = m
+        self.log_c0 = tabs["log_c0"]

@@ -1,0 +1,69 @@
+"""Seeded synthetic vibronic models in the reference's JSON format.
+
+Recipe (the shapes and value distributions of the benchmark configurations):
+  frequencies w_j ~ U[0.02, 0.30] eV; diagonal energies ~ U[0, 0.5] eV; symmetric off-diagonal
+  energies ~ N(0, sd_offdiag); linear couplings ~ N(0, 0.01) symmetrised in the surfaces;
+  quadratic couplings ~ N(0, sd_quadratic) symmetrised in the modes and in the surfaces, then
+  shrunk until 1/2 diag(w) + Q_aa is positive definite (margin: smallest eigenvalue at least
+  w_min / 8) for every surface.  The sampling model rho is the diagonal (harmonic) part of the
+  coupled model (vibronic_model_io.py:774-787).
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+
+from . import vibronic_io as vIO
+from .vibronic_io import VMK
+
+
+def make_coupled_model(A, N, seed, sd_offdiag=0.05, sd_linear=0.01, sd_quadratic=0.002,
+                       quadratic=True):
+    rng = np.random.default_rng(seed)
+    w = rng.uniform(0.02, 0.30, size=N)
+    E = np.zeros((A, A))
+    E[np.diag_indices(A)] = rng.uniform(0.0, 0.5, size=A)
+    off = rng.normal(0.0, sd_offdiag, size=(A, A))
+    iu = np.triu_indices(A, 1)
+    E[iu] = off[iu]
+    E[(iu[1], iu[0])] = off[iu]
+    L = rng.normal(0.0, sd_linear, size=(N, A, A))
+    L = 0.5 * (L + L.transpose(0, 2, 1))
+    Q = np.zeros((N, N, A, A))
+    if quadratic and sd_quadratic > 0:
+        Q = rng.normal(0.0, sd_quadratic, size=(N, N, A, A))
+        Q = 0.5 * (Q + Q.transpose(1, 0, 2, 3))
+        Q = 0.5 * (Q + Q.transpose(0, 1, 3, 2))
+        margin = w.min() / 8.0
+        for _ in range(200):
+            ok = all(np.linalg.eigvalsh(0.5 * np.diag(w) + Q[:, :, a, a]).min() >= margin
+                     for a in range(A))
+            if ok:
+                break
+            Q *= 0.8
+    return {VMK.N: N, VMK.A: A, VMK.E: E, VMK.w: w, VMK.G1: L, VMK.G2: Q}
+
+
+def diagonal_of(model):
+    out = {VMK.N: model[VMK.N], VMK.A: model[VMK.A]}
+    for key in (VMK.E, VMK.w, VMK.G1, VMK.G2):
+        v = model[key]
+        out[key] = np.diagonal(v, axis1=v.ndim - 2, axis2=v.ndim - 1).copy() if v.ndim >= 2 else v.copy()
+    return out
+
+
+def write_model_pair(FS, A, N, seed, **kw):
+    """Write coupled_model.json and the basic sampling_model.json of FS; returns the coupled dict."""
+    model = make_coupled_model(A, N, seed, **kw)
+    os.makedirs(os.path.dirname(FS.path_vib_model), exist_ok=True)
+    vIO.save_model_to_JSON(FS.path_vib_model, model)
+    vIO.create_basic_diagonal_model(FS)
+    return model
+
+
+#: benchmark configurations (sizes of the reference's headline runs)
+CONFIGS = {
+    1: dict(A=2, N=2, P=12, T=300.0, X=10_000, B=1_000),
+    2: dict(A=4, N=12, P=64, T=300.0, X=1_000_000, B=10_000),
+}

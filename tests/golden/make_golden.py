@@ -1,0 +1,247 @@
+"""Generate the golden fixtures under tests/golden/ from the reference implementation itself.
+
+Run in a container where the reference is mounted (default /root/reference):
+
+    python tests/golden/make_golden.py [path_to_reference]
+
+It (1) packs the reference's own known-answer data (tests/pimc/explicit_data/*) into
+explicit_example.npz, and (2) imports the unmodified reference engine from a temporary copy
+(stub modules stand in for matplotlib and `parse`, which the engine never calls), runs
+block_compute_pm, block_compute, the learned-proposal data path and the estimators on seeded
+synthetic models, and records the sampled q and every output into reference_runs.npz, with the
+model files as JSON text.  The fixtures are small; the GPU machine never needs the reference.
+"""
+from __future__ import annotations
+
+import glob
+import json
+import os
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from pibronic_gb300 import synthetic, vibronic_io  # noqa: E402
+
+
+def import_reference(ref_root):
+    tmp = tempfile.mkdtemp(prefix="pbr_ref_")
+    stubs = os.path.join(tmp, "stubs")
+    os.makedirs(os.path.join(stubs, "matplotlib"))
+    with open(os.path.join(stubs, "matplotlib", "__init__.py"), "w") as fh:
+        fh.write("def use(*a, **k):\n    pass\n")
+    open(os.path.join(stubs, "matplotlib", "pyplot.py"), "w").close()
+    with open(os.path.join(stubs, "parse.py"), "w") as fh:
+        fh.write("def parse(*a, **k):\n    raise NotImplementedError\n"
+                 "def search(*a, **k):\n    raise NotImplementedError\n"
+                 "def compile(*a, **k):\n    raise NotImplementedError\n")
+    shutil.copytree(os.path.join(ref_root, "pibronic"), os.path.join(tmp, "pibronic"))
+    sys.path[:0] = [stubs, tmp]
+    import warnings
+    warnings.simplefilter("ignore")
+    import pibronic.pimc.pimc as engine
+    import pibronic.stats.stats as st
+    import pibronic.stats.jackknife as jk
+    import pibronic.data.file_structure as fs
+    import pibronic.constants as const
+    return engine, st, jk, fs, const, tmp
+
+
+def explicit_example(ref_root):
+    src = os.path.join(ref_root, "tests", "pimc", "explicit_data")
+    out = {}
+    for path in sorted(glob.glob(os.path.join(src, "*.npy"))):
+        key = os.path.basename(path)[:-4].replace("(", "_").replace(")", "")
+        out[key] = np.load(path)
+    for name in ("coupled_model", "sampling_model"):
+        with open(os.path.join(src, name + ".json")) as fh:
+            out[name + "_json"] = np.array(fh.read())
+    np.savez_compressed(os.path.join(HERE, "explicit_example.npz"), **out)
+    return sorted(out)
+
+
+def write_models(root, case):
+    """Write the case's model files under root/data_set_0/{parameters,rho_0/parameters}."""
+    vib_dir = os.path.join(root, "data_set_0", "parameters")
+    rho_dir = os.path.join(root, "data_set_0", "rho_0", "parameters")
+    os.makedirs(vib_dir, exist_ok=True)
+    os.makedirs(rho_dir, exist_ok=True)
+    if "vib_json" in case:
+        vib_text, rho_text = case["vib_json"], case["rho_json"]
+    else:
+        model = synthetic.make_coupled_model(case["A"], case["N"], case["model_seed"],
+                                             sd_offdiag=case.get("sd_offdiag", 0.05),
+                                             sd_quadratic=case.get("sd_quadratic", 0.002))
+        if case.get("zero_diag_linear"):
+            # equal state shifts keep V symmetric when each surface slot holds R - d_a
+            # (the learned-proposal data path asserts that symmetry, pimc.py:1169)
+            for a in range(case["A"]):
+                model[vibronic_io.VMK.G1][:, a, a] = 0.0
+        rho = synthetic.diagonal_of(model)
+        extra = case.get("extra_rho_surfaces", 0)
+        if extra:
+            A, N = case["A"], case["N"]
+            VMK = vibronic_io.VMK
+            rho[VMK.A] = A + extra
+            rho[VMK.E] = np.concatenate([rho[VMK.E], 0.3 + 0.1 * np.arange(extra)])
+            rho[VMK.G1] = np.concatenate([rho[VMK.G1], 0.02 * np.ones((N, extra))], axis=1)
+            rho[VMK.G2] = np.zeros((N, N, A + extra))
+        vibronic_io.save_model_to_JSON(os.path.join(vib_dir, "coupled_model.json"), model)
+        vibronic_io.save_diagonal_model_to_JSON(os.path.join(rho_dir, "sampling_model.json"), rho)
+        with open(os.path.join(vib_dir, "coupled_model.json")) as fh:
+            vib_text = fh.read()
+        with open(os.path.join(rho_dir, "sampling_model.json")) as fh:
+            rho_text = fh.read()
+    with open(os.path.join(vib_dir, "coupled_model.json"), "w") as fh:
+        fh.write(vib_text)
+    with open(os.path.join(rho_dir, "sampling_model.json"), "w") as fh:
+        fh.write(rho_text)
+    return vib_text, rho_text
+
+
+def run_case(engine, fs, const, case):
+    root = tempfile.mkdtemp(prefix="pbr_case_")
+    vib_text, rho_text = write_models(root, case)
+    FS = fs.FileStructure(root, 0, 0)
+    FS.generate_model_hashes()
+    pm = case.get("pm", True)
+    beta = const.beta(case["T"])
+    data = engine.BoxDataPM(case.get("dbeta_rel", 1e-4) * beta) if pm else engine.BoxData()
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.hash_vib, data.hash_rho = FS.hash_vib, FS.hash_rho
+    A, N = json.loads(vib_text)["number of surfaces"], json.loads(vib_text)["number of modes"]
+    data.states, data.modes = A, N
+    data.samples, data.beads, data.temperature = case["X"], case["P"], case["T"]
+    data.block_size = case["B"]
+    data.blocks = data.samples // data.block_size
+    np.random.seed(case["rng_seed"])
+    recorded = []
+    original = engine.BoxData.transform_sampled_coordinates
+
+    def recording(self, sample_view):
+        original(self, sample_view)
+        recorded.append(self.qTensor[:, 0].copy())
+
+    engine.BoxData.transform_sampled_coordinates = recording
+    try:
+        import contextlib
+        import io
+        with contextlib.redirect_stdout(io.StringIO()):
+            data.preprocess()
+            result = engine.BoxResultPM(data=data) if pm else engine.BoxResult(data=data)
+            result.path_root = FS.path_rho_results
+            result.id_job = 0
+            (engine.block_compute_pm if pm else engine.block_compute)(data, result)
+    finally:
+        engine.BoxData.transform_sampled_coordinates = original
+    out = {"q": np.concatenate(recorded), "s_rho": result.scaled_rho.copy(),
+           "s_g": result.scaled_g.copy(), "beta": beta, "tau": data.tau,
+           "delta_beta": data.delta_beta if pm else 0.0,
+           "state_weight": data.rho.state_weight.copy(),
+           "sample_sources": data.rho.sample_sources.copy(),
+           "vib_json": np.array(vib_text), "rho_json": np.array(rho_text)}
+    if pm:
+        out["s_gP"] = result.scaled_gofr_plus.copy()
+        out["s_gM"] = result.scaled_gofr_minus.copy()
+    shutil.rmtree(root, ignore_errors=True)
+    return out
+
+
+def run_ml_case(engine, fs, case):
+    """block_compute_gR_from_raw_samples + block_compute_rhoR_from_input_samples."""
+    root = tempfile.mkdtemp(prefix="pbr_ml_")
+    vib_text, rho_text = write_models(root, case)
+    FS = fs.FileStructure(root, 0, 0)
+    FS.generate_model_hashes()
+    data = engine.BoxData.from_FileStructure(FS)
+    data.hash_vib, data.hash_rho = FS.hash_vib, FS.hash_rho
+    data.samples, data.beads, data.temperature = case["X"], case["P"], case["T"]
+    data.block_size = case["B"]
+    data.blocks = data.samples // data.block_size
+    np.random.seed(case["rng_seed"])
+    import contextlib
+    import io
+    with contextlib.redirect_stdout(io.StringIO()):
+        data.preprocess()
+        result = engine.BoxResult(data=data)
+        result.id_job = 0
+        result.path_root = FS.path_vib_results
+        engine.block_compute_gR_from_raw_samples(data, result)
+        g = result.scaled_g.copy()
+        with np.load(os.path.join(FS.path_vib_results,
+                                  f"P{case['P']}_T{case['T']:.2f}_J0_training_data_input.npz")) as d:
+            R = d["input_R_values"].copy()
+        res2 = engine.BoxResult(data=data)
+        engine.block_compute_rhoR_from_input_samples(data, res2, R)
+    shutil.rmtree(root, ignore_errors=True)
+    return {"R": R, "g": g, "rho": res2.scaled_rho.copy(), "vib_json": np.array(vib_text),
+            "rho_json": np.array(rho_text)}
+
+
+CASES = {
+    # BASELINE config 1 shapes: A=2, N=2, P=12, T=300 K, quadratic terms, dbeta = 1e-4 beta
+    "cfg1": dict(A=2, N=2, P=12, T=300.0, X=400, B=100, model_seed=11, rng_seed=1234),
+    # config 2 shapes at a small sample count: A=4, N=12, P=64
+    "cfg2": dict(A=4, N=12, P=64, T=300.0, X=60, B=20, model_seed=22, rng_seed=4321),
+    # config 2 at the low temperature of its sweep
+    "cfg2_cold": dict(A=4, N=12, P=64, T=100.0, X=40, B=20, model_seed=23, rng_seed=99),
+    # odd bead count, three surfaces, strong off-diagonal couplings
+    "odd": dict(A=3, N=5, P=7, T=250.0, X=50, B=25, model_seed=5, rng_seed=77, sd_offdiag=0.1),
+    # plain block_compute (no beta +- db)
+    "plain": dict(A=2, N=3, P=16, T=300.0, X=50, B=25, model_seed=8, rng_seed=31, pm=False),
+    # sampling model with more surfaces than the coupled model (qTempTensor path)
+    "arho": dict(A=2, N=3, P=10, T=300.0, X=60, B=30, model_seed=9, rng_seed=55, extra_rho_surfaces=2),
+    # default delta_beta of the reference (2e-4 absolute) instead of 1e-4 beta
+    "single_surface": dict(A=1, N=4, P=8, T=300.0, X=40, B=20, model_seed=3, rng_seed=8),
+}
+
+
+def main(ref_root="/root/reference"):
+    keys = explicit_example(ref_root)
+    print("explicit_example.npz:", keys)
+    engine, st, jk, fs, const, tmp = import_reference(ref_root)
+    runs = {}
+    for name, case in CASES.items():
+        out = run_case(engine, fs, const, case)
+        for k, v in out.items():
+            runs[f"{name}/{k}"] = v
+        print(name, {k: np.shape(v) for k, v in out.items()})
+    # reference test models (tests/test_models/data_set_1/rho_1), block_compute_pm
+    with open(os.path.join(ref_root, "tests/test_models/data_set_1/parameters/coupled_model.json")) as fh:
+        vt = fh.read()
+    with open(os.path.join(ref_root, "tests/test_models/data_set_1/rho_1/parameters/sampling_model.json")) as fh:
+        rt = fh.read()
+    out = run_case(engine, fs, const, dict(vib_json=vt, rho_json=rt, P=12, T=300.0, X=40, B=20,
+                                            rng_seed=242351, dbeta_rel=const.delta_beta / const.beta(300.0)))
+    for k, v in out.items():
+        runs[f"testmodel/{k}"] = v
+    # estimators on the cfg1 run (stats.py:38-130, jackknife.py:60-105)
+    c = {k.split("/")[1]: v for k, v in runs.items() if k.startswith("cfg1/")}
+    X, T, dB = len(c["s_rho"]), 300.0, float(c["delta_beta"])
+    terms = st.calculate_basic_property_terms(dB, c["s_rho"], c["s_g"], c["s_gP"], c["s_gM"])
+    basic = st.estimate_basic_properties(X, T, *terms)
+    jkt = jk.calculate_jackknife_terms(X, terms)
+    jkd = jk.estimate_jackknife(X, T, dB, basic, *jkt)
+    for k, v in basic.items():
+        runs[f"stats/basic/{k}"] = np.float64(v)
+    for k, v in jkd.items():
+        runs[f"stats/jk/{k}"] = np.float64(v)
+    # learned-proposal data path
+    ml = run_ml_case(engine, fs, dict(A=2, N=3, P=8, T=300.0, X=30, B=15, model_seed=17, rng_seed=2024,
+                                      zero_diag_linear=True))
+    for k, v in ml.items():
+        runs[f"ml/{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "reference_runs.npz"), **runs)
+    with open(os.path.join(HERE, "cases.json"), "w") as fh:
+        json.dump(CASES, fh, indent=1)
+    shutil.rmtree(tmp, ignore_errors=True)
+    print("wrote", os.path.join(HERE, "reference_runs.npz"))
+
+
+if __name__ == "__main__":
+    main(*sys.argv[1:])
