@@ -1,0 +1,413 @@
+#!/usr/bin/env python
+"""Benchmark: effective samples per second of the PIMC block evaluation on GB300.
+
+Workload (the headline configuration): synthetic seeded vibronic model A=4 surfaces, N=12 modes,
+P=64 beads, T=300 K, delta_beta = 1e-4 beta, X = 1e6 samples per step per GPU, plain rho
+proposal.  One step = one fused launch that draws and evaluates X samples (rho, g, g(beta+-db))
+plus the two FP64 reduction passes that turn them into Z, E, Cv with jackknife errors.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  value = ESS/s summed over ranks, ESS = (sum w)^2 / sum w^2 of w = g/rho.
+--impl reference times the CPU restatement of the reference engine (the oracle port of
+pibronic/pimc/pimc.py block_compute_pm) on all host cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+METRIC = "ESS/sec for Z,E,Cv at 1e-3 rel err: learned vs plain rho, 1 GB300"
+A_, N_, P_, T_ = 4, 12, 64, 300.0
+MODEL_SEED = 20240
+
+
+def flops_per_sample(A, N, P):
+    """Algorithmic work per sample: ring transform 2NP^2, four O sets 24ANP, V P(2N^2A^2 + 2NA^2),
+    eigh 10PA^3, M 2PA^3, three ring products 3P(2A^3 + A^2)."""
+    return (2 * N * P * P + 24 * A * N * P + P * (2 * N * N * A * A + 2 * N * A * A)
+            + 10 * P * A ** 3 + 2 * P * A ** 3 + 3 * P * (2 * A ** 3 + A * A))
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU side: the oracle port (reference arm and cpu_baseline)
+# ---------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    vib_text, rho_text, X, P, T, db_rel, seed = args
+    import numpy as np
+    from oracle import pimc_oracle as po
+    np.random.seed(seed)
+    vib = po.model_from_text(vib_text)
+    rho = po.model_from_text(rho_text, diagonal=True)
+    beta = po.beta_of(T)
+    box = po.OracleBox(vib, rho, X, min(X, 10_000), P, T, delta_beta=db_rel * beta)
+    t0 = time.perf_counter()
+    res = box.block_compute(plus_minus=True)
+    el = time.perf_counter() - t0
+    return el, res["s_rho"], res["s_g"], res["s_gP"], res["s_gM"]
+
+
+def cpu_port_run(vib_text, rho_text, samples_per_worker, workers, seed0=0):
+    """One bounded sample of the workload on `workers` processes (spawned); returns
+    (samples/s, ESS/s, ESS/X, wall seconds, cpu seconds)."""
+    import multiprocessing as mp
+    import numpy as np
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"          # one BLAS thread per spawned process
+    ctx = mp.get_context("spawn")
+    jobs = [(vib_text, rho_text, samples_per_worker, P_, T_, 1e-4, 1000 + seed0 + i)
+            for i in range(workers)]
+    with ctx.Pool(workers) as pool:
+        t0 = time.perf_counter()
+        outs = pool.map(_cpu_worker, jobs)
+        wall = time.perf_counter() - t0
+    busy = max(o[0] for o in outs)
+    r = np.concatenate([o[2] / o[1] for o in outs])
+    ess_frac = r.sum() ** 2 / (r * r).sum() / len(r)
+    sps = len(r) / busy
+    return sps, sps * ess_frac, ess_frac, wall, sum(o[0] for o in outs)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def model_texts():
+    from pibronic_gb300 import synthetic, vibronic_io
+    root = tempfile.mkdtemp(prefix="pbr_bench_")
+    from pibronic_gb300.file_structure import FileStructure
+    FS = FileStructure(root, 0, 0)
+    synthetic.write_model_pair(FS, A_, N_, MODEL_SEED)
+    with open(FS.path_vib_model) as fh:
+        vt = fh.read()
+    with open(FS.path_rho_model) as fh:
+        rt = fh.read()
+    return FS, vt, rt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    _, vt, rt = model_texts()
+    cores = host_cores()
+    per_worker = args.cpu_samples
+    for w in range(args.warmup):
+        cpu_port_run(vt, rt, max(20, per_worker // 4), cores, seed0=10_000 * (w + 1))
+    vals, sps_l, fr = [], [], []
+    t_all = time.perf_counter()
+    for s in range(args.steps):
+        sps, ess_s, ess_frac, wall, cpu = cpu_port_run(vt, rt, per_worker, cores, seed0=100 * s)
+        vals.append(ess_s)
+        sps_l.append(sps)
+        fr.append(ess_frac)
+    elapsed = time.perf_counter() - t_all
+    value = statistics.mean(vals)
+    sample = (f"{args.steps} steps x {cores} spawned processes x {per_worker} samples of the "
+              f"workload (oracle port of block_compute_pm, FP64 numpy), preprocess excluded")
+    line = {
+        "metric": METRIC, "value": value, "unit": "ESS/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(),
+        "samples_per_s": statistics.mean(sps_l), "ess_per_sample": statistics.mean(fr),
+        "cpu_baseline": {"value": value, "unit": "ESS/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "ESS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config():
+    return {"workload": f"plain-rho PIMC block evaluation (block_compute_pm): A={A_} N={N_} P={P_} "
+                        f"T={T_:.0f}K dbeta=1e-4*beta, 1e6 samples per step per GPU",
+            "A": A_, "N": N_, "P": P_, "T": T_, "X_per_gpu": 1_000_000, "model_seed": MODEL_SEED,
+            "proposal": "rho (plain)", "l2": "flushed between timed steps (256 MB write)"}
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index, self.proc, self.path = index, None, None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="pbr_clk_", suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                try:
+                    rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+                except ValueError:
+                    pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, f in rows for i, v in enumerate(f) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def fp32_peak(torch, lib, stream):
+    """Measured FP32 FMA peak (TFLOP/s) of this GPU with the library's FFMA probe."""
+    from pibronic_gb300 import _native
+    import ctypes
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    out = torch.empty(sms * 8, dtype=torch.float32, device="cuda")
+    fl = ctypes.c_double()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _native.check(lib.pbr_fma_probe(_native.ptr(out), sms * 8, 4096, ctypes.byref(fl),
+                                        _native.stream_handle(stream)), "fma probe")
+        e1.record(stream)
+        e1.synchronize()
+        best = max(best, fl.value / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def read_traffic():
+    """DRAM bytes per fused launch from the committed ncu summary, if present."""
+    path = os.path.join(HERE, "profiles", "fused_config2_ncu.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from pibronic_gb300 import _native, pimc, stats
+    from pibronic_gb300.build import build
+    lib = _native.load(build() if rank == 0 and world == 1 else None)
+    X = args.samples
+    FS, vt, rt = model_texts() if rank == 0 else (None, None, None)
+    if world > 1:
+        obj = [vt, rt]
+        dist.broadcast_object_list(obj, src=0)
+        vt, rt = obj
+        root = tempfile.mkdtemp(prefix=f"pbr_bench_r{rank}_")
+        from pibronic_gb300.file_structure import FileStructure
+        FS = FileStructure(root, 0, 0)
+        open(FS.path_vib_model, "w").write(vt)
+        open(FS.path_rho_model, "w").write(rt)
+    # the public API: BoxDataPM from the model files, preprocess builds the device plan
+    from pibronic_gb300 import constants
+    beta = constants.beta(T_)
+    data = pimc.BoxDataPM(1e-4 * beta)
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.states, data.modes, data.beads, data.temperature = A_, N_, P_, T_
+    data.samples, data.block_size = X, 10_000
+    data.blocks = X // data.block_size
+    data.seed = 0x5EED + rank
+    data.preprocess()
+    plan = data.plan
+    stream = torch.cuda.current_stream()
+    dev = torch.device("cuda", local)
+    bufs = {k: torch.empty(X, dtype=torch.float64, device=dev) for k in ("s_rho", "s_g", "s_gp", "s_gm")}
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    o = _native.PbrOutputs()
+    o.s_rho, o.s_g = bufs["s_rho"].data_ptr(), bufs["s_g"].data_ptr()
+    o.s_gp, o.s_gm = bufs["s_gp"].data_ptr(), bufs["s_gm"].data_ptr()
+    o.status = status.data_ptr()
+    red = stats.DeviceReducer(X)
+    sh = _native.stream_handle(stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    hist = torch.empty((args.steps + args.warmup, 12), dtype=torch.float64, device=dev)
+
+    def step(i, e_k0=None, e_k1=None):
+        offset = (i * world + rank) * X
+        if e_k0 is not None:
+            e_k0.record(stream)
+        _native.check(lib.pbr_sample_eval(plan.struct, data.seed, offset, X, o, sh), "sample_eval")
+        if e_k1 is not None:
+            e_k1.record(stream)
+        red.launch(bufs["s_rho"], bufs["s_g"], bufs["s_gp"], bufs["s_gm"], data.delta_beta, T_, stream)
+        hist[i, :7].copy_(red.moments)
+        hist[i, 7:].copy_(red.jk)
+
+    for w in range(args.warmup):
+        step(w)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for s in range(args.steps):
+        flush.fill_(float(s))                      # L2 flush between timed steps (untimed)
+        e0, e1, e2 = ev[s]
+        step(args.warmup + s, e0, e1)
+        e2.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e2) for e0, _, e2 in ev]
+    kern_ms = [e0.elapsed_time(e1) for e0, e1, _ in ev]
+    ms_step = sum(step_ms) / len(step_ms)
+    ms_kern = sum(kern_ms) / len(kern_ms)
+    if int(status.item()) != 0:
+        raise RuntimeError("non-finite results in the timed steps")
+    H = hist.cpu().numpy()[args.warmup:]
+    ests = [stats.estimates_from_moments(h[:7], h[7:], T_) for h in H]
+    ess = statistics.mean(e["ESS"] for e in ests)
+    t = torch.tensor([ms_step, ess, ms_kern], dtype=torch.float64, device=dev)
+    if dist:
+        tmax = t.clone()
+        dist.all_reduce(tmax[:1], op=dist.ReduceOp.MAX)
+        tsum = t.clone()
+        dist.all_reduce(tsum[1:2])
+        ms_step, ess_total = float(tmax[0]), float(tsum[1])
+    else:
+        ess_total = ess
+    value = ess_total / (ms_step * 1e-3)
+    sps = X * world / (ms_step * 1e-3)
+    e = ests[-1]
+    rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
+           "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
+    t_1e3 = {k: X * world * (v / 1e-3) ** 2 / sps for k, v in rel.items()}
+
+    # ---- e2e through the public API with host buffers ----
+    e2e_val, h2d, d2h = None, 0, 0
+    pinned = {k: torch.empty(X, dtype=torch.float64, pin_memory=True) for k in bufs}
+    tab_host = {k: v.cpu().pin_memory() for k, v in plan.tensors.items()}
+    h2d = sum(v.numel() * v.element_size() for v in tab_host.values())
+    d2h = sum(v.numel() * v.element_size() for v in pinned.values()) + 12 * 8
+    e2e_times = []
+    for s in range(max(2, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k, v in tab_host.items():                 # the step's inputs: model tables
+            plan.tensors[k].copy_(v, non_blocking=True)
+        _native.check(lib.pbr_sample_eval(plan.struct, data.seed + 1, (s * world + rank) * X, X, o, sh),
+                      "sample_eval")
+        red.launch(bufs["s_rho"], bufs["s_g"], bufs["s_gp"], bufs["s_gm"], data.delta_beta, T_, stream)
+        for k in bufs:
+            pinned[k].copy_(bufs[k], non_blocking=True)
+        mom = red.moments.cpu()
+        jkv = red.jk.cpu()
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+        ee = stats.estimates_from_moments(mom.numpy(), jkv.numpy(), T_)
+    e2e_t = statistics.mean(e2e_times)
+    if dist:
+        tt = torch.tensor([e2e_t], dtype=torch.float64, device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_t = float(tt[0])
+    e2e_val = ess_total / e2e_t
+
+    # ---- roofline of the fused kernel ----
+    W = flops_per_sample(A_, N_, P_)
+    achieved = W * X / (ms_kern * 1e-3) / 1e12
+    peak = fp32_peak(torch, lib, stream)
+    traffic = read_traffic()
+    roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "peak_source": "FP32 FFMA probe (pbr_fma_probe) measured in this run; "
+                           "MEASURED_PEAKS.json has only HBM copy and bf16 tensor peaks",
+            "flops_per_sample": W, "kernel_ms": ms_kern,
+            "hbm_frac_of_measured": (32.0 * X / (ms_kern * 1e-3) / 1e9) / 6801.7}
+    line = {
+        "metric": METRIC, "value": value, "unit": "ESS/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+        "samples_per_s": sps, "ess_per_sample": ess_total / (X * world),
+        "rel_err": rel, "time_to_1e-3_s": t_1e3,
+        "estimates": {k: e[k] for k in ("Z", "Z error", "E", "jk_E", "jk_E error", "Cv", "jk_Cv", "jk_Cv error")},
+        "roofline": roof,
+        "e2e": {"value": e2e_val, "unit": "ESS/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step": 1e3 * e2e_t},
+        "clocks": clk, "gpu_launches": 5 * args.steps,
+    }
+    # ---- CPU baseline: the oracle port on the host cores, rank 0 at N=1 only ----
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = host_cores()
+        sps_c, ess_c, frac_c, wall, cpu = cpu_port_run(vt, rt, args.cpu_samples, cores)
+        line["cpu_baseline"] = {
+            "value": ess_c, "unit": "ESS/s", "cores": cores, "kind": "port",
+            "samples_per_s": sps_c,
+            "sample": f"{cores} spawned processes x {args.cpu_samples} samples of the same workload "
+                      f"(oracle port of block_compute_pm, FP64 numpy), {cpu:.1f} s of CPU work"}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--samples", type=int, default=1_000_000, help="samples per step per GPU")
+    ap.add_argument("--cpu-samples", type=int, default=400, help="samples per host process (CPU legs)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

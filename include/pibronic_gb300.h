@@ -179,7 +179,7 @@ int pbr_numerator(const double* eigvals, const double* eigvecs, const double* O,
  *   deviations from the mean), with r = g/rho, s1 = (g+ - g-)/(2 db rho),
  *   s2 = (g+ - 2g + g-)/(db^2 rho) (stats.py:38-55).  Z = mean r and its error
  *   sqrt(M2 r / n) / sqrt(n - 1) (stats.py:84-90), E = -mean s1 / Z, Cv = (mean s2 / Z - E^2)/(kB T^2).
- * scratch must hold 7 * pbr_reduce_blocks(X) doubles.
+ * scratch must hold 9 * pbr_reduce_blocks(X) doubles.
  * Replaces the numpy reductions of stats.estimate_basic_properties (stats.py:84-123).
  */
 int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
@@ -195,7 +195,7 @@ int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
  *   dE_i = (S_r s1_i - S_1 r_i) / (S_r (S_r - r_i)) * (-1)
  *   dC_i = ((S_r s2_i - S_2 r_i) / (S_r (S_r - r_i)) - dE_i (2 E0 + dE_i)) / (kB T^2)
  * into out[0..4] = n, mean dE, M2 dE, mean dC, M2 dC (same merge as pbr_reduce_terms).
- * totals = {S_r, S_1, S_2}.  scratch must hold 5 * pbr_reduce_blocks(X) doubles.
+ * totals = {S_r, S_1, S_2}.  scratch must hold 6 * pbr_reduce_blocks(X) doubles.
  */
 int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s_gp,
                          const double* s_gm, int64_t X, double delta_beta, double kB_T2,
@@ -203,6 +203,14 @@ int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s
 
 /* Number of partial blocks the reductions use for X samples. */
 int64_t pbr_reduce_blocks(int64_t X);
+
+/*
+ * FP32 FMA throughput probe: blocks x 256 threads, each running 8 independent FMA chains for
+ * 16 * iters steps; *flops gets the flop count of the launch.  Time it with events to get the
+ * CUDA-core FP32 peak the fused kernel is compared against.  No counterpart in the reference
+ * (a measurement utility).
+ */
+int pbr_fma_probe(float* out, int32_t blocks, int32_t iters, double* flops, void* stream);
 
 /* Library version string and the SM architecture it was built for. */
 const char* pbr_version(void);

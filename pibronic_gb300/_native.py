@@ -25,7 +25,8 @@ EXPORTED = (
     "pbr_sample_eval", "pbr_sample_q", "pbr_eval_q", "pbr_eval_q_f32",
     "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_divide_o_matrix", "pbr_denominator",
     "pbr_coupling_eigh", "pbr_numerator",
-    "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_version",
+    "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_fma_probe",
+    "pbr_version",
 )
 
 
@@ -73,6 +74,7 @@ def _declare(lib):
         "pbr_reduce_terms": (C.c_int, [vp, vp, vp, vp, i64, f64, vp, vp, vp]),
         "pbr_reduce_jackknife": (C.c_int, [vp, vp, vp, vp, i64, f64, f64, vp, vp, vp, vp]),
         "pbr_reduce_blocks": (i64, [i64]),
+        "pbr_fma_probe": (C.c_int, [vp, i32, i32, C.POINTER(f64), vp]),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

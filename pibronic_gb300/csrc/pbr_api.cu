@@ -10,6 +10,8 @@ template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t)
 
 namespace {
 
+constexpr int kMaxSmem = 227 * 1024;   // opt-in shared memory per CTA on sm_103a
+
 int pow2ceil(int x) {
     int p = 1;
     while (p < x) p <<= 1;
@@ -51,14 +53,25 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     a.key0 = static_cast<uint32_t>(seed);
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
-    a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
-    a.logG = ilog2(a.G);
-    a.C = (m.P + a.G - 1) / a.G;
-    if (qmode == kSample && a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;   // P > 256
-    a.S = kThreads / a.G;
     const int A2 = npair(m.A);
     a.a2p = (A2 + 3) / 4 * 4;
     a.qstride = m.N * m.P + 1;
+    // threads per sample: enough that each owns <= kMaxChunk beads, more (up to a warp) when
+    // the per-CTA shared memory of S = kThreads / G samples would not fit
+    const int esz = m.precision == 32 ? 4 : 8;
+    a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
+    while (true) {
+        a.S = kThreads / a.G;
+        const SmemPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.a2p, a.S, a.qstride);
+        if (plan.total_bytes <= kMaxSmem || a.G == 32) {
+            if (plan.total_bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
+            break;
+        }
+        a.G *= 2;
+    }
+    a.logG = ilog2(a.G);
+    a.C = (m.P + a.G - 1) / a.G;
+    if (qmode == kSample && a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;   // P > 256
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (m.A) {
         case 1: return launch_fused<1>(m.K, qmode, m.precision, a, st);
@@ -107,14 +120,20 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
     a.key0 = static_cast<uint32_t>(seed);
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
+    a.qstride = m.N * m.P + 1;
+    const size_t esz = m.precision == 32 ? sizeof(float) : sizeof(double);
     a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
+    int bytes = 0;
+    while (true) {
+        a.S = kThreads / a.G;
+        bytes = static_cast<int>((align_up(2 * m.P, 4) + a.S * a.qstride) * esz);
+        if (bytes <= kMaxSmem || a.G == 32) break;
+        a.G *= 2;
+    }
+    if (bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
     a.logG = ilog2(a.G);
     a.C = (m.P + a.G - 1) / a.G;
     if (a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;
-    a.S = kThreads / a.G;
-    a.qstride = m.N * m.P + 1;
-    const size_t esz = m.precision == 32 ? sizeof(float) : sizeof(double);
-    const int bytes = static_cast<int>((align_up(2 * m.P, 4) + a.S * a.qstride) * esz);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto go = [&](auto kern) -> int {
         if (bytes > 48 * 1024 &&

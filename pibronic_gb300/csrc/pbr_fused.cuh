@@ -42,22 +42,22 @@ struct FusedArgs {
 
 __host__ __device__ inline int align_up(int x, int a) { return (x + a - 1) / a * a; }
 
-// Shared-memory plan (in elements of T unless stated); identical on host and device.
-template <int A, int K, int QM, typename T>
+// Shared-memory plan (in elements of the table type, esz bytes each); identical on host and device.
 struct SmemPlan {
     int cs, th, c, d, e, l, qq, rcs, rth, rc, rd, trig, q, qlo, total_bytes;
-    __host__ __device__ SmemPlan(int N, int P, int a2p, int S, int qstride) {
-        constexpr int A2 = npair(A);
+    __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int a2p, int S,
+                                 int qstride) {
+        const int A2 = npair(A);
         const int N2 = npair(N);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
         cs = take((K + 1) * N); th = take((K + 1) * N); c = take((K + 1) * A); d = take(A * N);
         e = take(A2); l = take(N * A2); qq = take(N2 * a2p);
         rcs = take(N); rth = take(N); rc = take(A); rd = take(A * N);
-        trig = take(QM == kSample ? 2 * P : 0);
+        trig = take(qm == kSample ? 2 * P : 0);
         q = take(S * qstride);
-        qlo = take((QM == kQ64 && sizeof(T) == 4) ? S * qstride : 0);
-        total_bytes = o * static_cast<int>(sizeof(T));
+        qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
+        total_bytes = o * esz;
     }
 };
 
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
     const pbr_model& m = args.m;
     const int N = m.N, P = m.P, nfill = m.n_fill_rho;
     const int G = args.G, C = args.C, S = args.S;
-    const SmemPlan<A, K, QM, T> plan(N, P, args.a2p, S, args.qstride);
+    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, args.a2p, S, args.qstride);
     T* s_cs = sm + plan.cs;  T* s_th = sm + plan.th;  T* s_c = sm + plan.c;  T* s_d = sm + plan.d;
     T* s_e = sm + plan.e;    T* s_l = sm + plan.l;    T* s_qq = sm + plan.qq;
     T* s_rcs = sm + plan.rcs; T* s_rth = sm + plan.rth; T* s_rc = sm + plan.rc; T* s_rd = sm + plan.rd;

@@ -1,0 +1,156 @@
+"""Estimators of Z, E, Cv: the reference's functions (pibronic/stats/stats.py:38-333) on host FP64
+arrays, plus the device path that reduces the per-sample outputs on the GPU.
+
+Device path: ``device_estimates(rho, g, gp, gm, T, delta_beta)`` takes CUDA tensors (the
+``result.device`` arrays block_compute_pm leaves behind) and runs two FP64 reduction kernels:
+the moments of r = g/rho, s1, s2 (pbr_reduce_terms) and the jackknife pass over the leave-one-out
+estimators (pbr_reduce_jackknife).  Only a handful of doubles come back to the host.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import _native
+from . import jackknife as jk
+from .constants import boltzman
+
+__all__ = ["calculate_alpha_terms", "add_harmonic_contribution", "estimate_basic_properties",
+           "calculate_basic_property_terms", "device_estimates", "ess"]
+
+
+def calculate_basic_property_terms(*args):
+    """g/rho, (g+ - g-)/(2 db rho), (g+ - 2g + g-)/(db^2 rho) (stats.py:38-55)."""
+    delta_beta, rho, g, g_plus, g_minus = args
+    ratio = g / rho
+    d1 = (g_plus - g_minus) / rho / (2.0 * delta_beta)
+    d2 = (g_plus - (2.0 * g) + g_minus) / rho / pow(delta_beta, 2)
+    return [ratio, d1, d2]
+
+
+def calculate_alpha_terms(*args):
+    """stats.py:58-81."""
+    delta_beta, rho, g, g_plus, g_minus, alpha_plus, alpha_minus = args
+    ratio, rp, rm = g / rho, g_plus / rho, g_minus / rho
+    d1 = (np.mean(rp) * np.mean(alpha_plus) - np.mean(rm) * np.mean(alpha_minus)) / (2.0 * delta_beta)
+    d2 = (np.mean(rp) * np.mean(alpha_plus) - 2.0 * np.mean(ratio)
+          + np.mean(rm) * np.mean(alpha_minus)) / pow(delta_beta, 2)
+    return [ratio, d1, d2, rp, alpha_plus, rm, alpha_minus]
+
+
+def basic_estimate_Z_monte_carlo(g_over_rho, number_of_samples):
+    Z = np.mean(g_over_rho)
+    return Z, np.std(g_over_rho, ddof=0) / np.sqrt(number_of_samples - 1)
+
+
+def basic_estimate_internal_energy(first_symmetric_derivative, Z_MC):
+    return -1.0 * np.mean(first_symmetric_derivative) / np.mean(Z_MC), 0.0
+
+
+def basic_estimate_heat_capacity(second_symmetric_derivative, Z_MC, internal_energy, temperature):
+    Cv = (np.mean(second_symmetric_derivative) / np.mean(Z_MC) - pow(internal_energy, 2.0))
+    return Cv / (boltzman * pow(temperature, 2.0)), 0.0
+
+
+def estimate_basic_properties(*args):
+    """Z, E, Cv and errors (stats.py:109-123)."""
+    X, T, g_r, sym1, sym2 = args
+    Z, Z_err = basic_estimate_Z_monte_carlo(g_r, X)
+    E, E_err = basic_estimate_internal_energy(sym1, Z)
+    Cv, Cv_err = basic_estimate_heat_capacity(sym2, Z, E, T)
+    return {"Z": Z, "Z error": Z_err, "E": E, "E error": E_err, "Cv": Cv, "Cv error": Cv_err}
+
+
+def add_harmonic_contribution(input_dict, E_sampling, Cv_sampling):
+    """stats.py:126-130."""
+    input_dict["E"] += E_sampling
+    input_dict["Cv"] += Cv_sampling
+
+
+def basic_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta):
+    """stats.py:271-301 (with the run's delta_beta passed explicitly)."""
+    data = [pimc_result.scaled_rho, pimc_result.scaled_g, pimc_result.scaled_gofr_plus,
+            pimc_result.scaled_gofr_minus]
+    X = pimc_result.samples
+    terms = calculate_basic_property_terms(delta_beta, *data)
+    jk_terms = jk.calculate_jackknife_terms(X, terms)
+    basic = estimate_basic_properties(X, temperature, *terms)
+    jkd = jk.estimate_jackknife(X, temperature, delta_beta, basic, *jk_terms)
+    add_harmonic_contribution(basic, analytic_data["E"], analytic_data["Cv"])
+    add_harmonic_contribution(jkd, analytic_data["E"], analytic_data["Cv"])
+    out = dict(basic)
+    out.update({"jk_" + k: v for k, v in jkd.items()})
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# device path
+# ---------------------------------------------------------------------------------------------
+class DeviceReducer:
+    """Preallocated scratch for the reduction kernels of X samples (no allocation per call)."""
+
+    def __init__(self, X):
+        torch = _native.require_cuda()
+        lib = _native.load()
+        nb = int(lib.pbr_reduce_blocks(int(X)))
+        self.X = X
+        self.scratch = torch.empty(nb * 9, dtype=torch.float64, device="cuda")
+        self.moments = torch.empty(7, dtype=torch.float64, device="cuda")
+        self.jk = torch.empty(5, dtype=torch.float64, device="cuda")
+        self.totals = torch.empty(3, dtype=torch.float64, device="cuda")
+
+    def launch(self, rho, g, gp, gm, delta_beta, temperature, stream=None):
+        """Queue both passes on the stream (nothing is read back)."""
+        lib = _native.load()
+        sh = _native.stream_handle(stream)
+        p = _native.ptr
+        _native.check(lib.pbr_reduce_terms(p(rho), p(g), p(gp), p(gm), self.X, float(delta_beta),
+                                           p(self.scratch), p(self.moments), sh), "reduce_terms")
+        if gp is None:
+            return 3
+        # totals S_r, S_1, S_2 = n * mean, computed on the device without a host round trip
+        self.totals.copy_(self.moments[[1, 3, 5]] * self.moments[0])
+        kT2 = boltzman * temperature ** 2
+        _native.check(lib.pbr_reduce_jackknife(p(rho), p(g), p(gp), p(gm), self.X, float(delta_beta),
+                                               float(kT2), p(self.totals), p(self.scratch),
+                                               p(self.jk), sh), "reduce_jackknife")
+        return 5
+
+    def read(self, temperature):
+        m = self.moments.cpu().numpy()
+        j = self.jk.cpu().numpy()
+        return estimates_from_moments(m, j, temperature)
+
+
+def estimates_from_moments(m, j, temperature):
+    """Z, E, Cv (basic, stats.py:84-123) and the jackknife E, Cv with errors (jackknife.py:77-105)
+    from the device moments; also the effective sample size (sum r)^2 / sum r^2."""
+    n, mr, m2r, m1, _, m2, _ = (float(x) for x in m)
+    Z = mr
+    Z_err = math.sqrt(max(m2r, 0.0) / n) / math.sqrt(n - 1)
+    E = -m1 / Z
+    Cv = (m2 / Z - E * E) / (boltzman * temperature ** 2)
+    out = {"X": n, "Z": Z, "Z error": Z_err, "E": E, "E error": 0.0, "Cv": Cv, "Cv error": 0.0,
+           "ESS": (n * mr) ** 2 / (m2r + n * mr * mr)}
+    if j is not None and len(j) == 5 and n > 1:
+        _, mdE, m2dE, mdC, m2dC = (float(x) for x in j)
+        # f_i = E0 + dE_i; jackknife E = X E - (X-1) mean f = E0 - (X-1) mean dE
+        out["jk_E"] = E - (n - 1.0) * mdE
+        out["jk_E error"] = math.sqrt(n - 1.0) * math.sqrt(max(m2dE, 0.0) / (n - 1.0))
+        out["jk_Cv"] = Cv - (n - 1.0) * mdC
+        out["jk_Cv error"] = math.sqrt(n - 1.0) * math.sqrt(max(m2dC, 0.0) / (n - 1.0))
+    return out
+
+
+def device_estimates(rho, g, gp, gm, temperature, delta_beta):
+    """Z, E, Cv, jackknife errors and ESS from CUDA tensors of per-sample outputs."""
+    red = DeviceReducer(rho.shape[0])
+    red.launch(rho, g, gp, gm, delta_beta, temperature)
+    return red.read(temperature)
+
+
+def ess(weights):
+    """Effective sample size (sum w)^2 / sum w^2 (host)."""
+    w = np.asarray(weights, dtype=np.float64)
+    return w.sum() ** 2 / (w * w).sum()
