@@ -192,8 +192,8 @@ int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
  *   f_E,i = -(S_1 - s1_i)/(S_r - r_i),  f_C,i = ((S_2 - s2_i)/(S_r - r_i) - f_E,i^2)/(kB T^2).
  * The kernel reduces their deviations from the full-sample values, written without the
  * cancellation of the direct difference:
- *   dE_i = (S_r s1_i - S_1 r_i) / (S_r (S_r - r_i)) * (-1)
- *   dC_i = ((S_r s2_i - S_2 r_i) / (S_r (S_r - r_i)) - dE_i (2 E0 + dE_i)) / (kB T^2)
+ *   dE_i = f_E,i - E0 = (S_r s1_i - S_1 r_i) / (S_r (S_r - r_i))
+ *   dC_i = f_C,i - C0 = (-(S_r s2_i - S_2 r_i) / (S_r (S_r - r_i)) - dE_i (2 E0 + dE_i)) / (kB T^2)
  * into out[0..4] = n, mean dE, M2 dE, mean dC, M2 dC (same merge as pbr_reduce_terms).
  * totals = {S_r, S_1, S_2}.  scratch must hold 6 * pbr_reduce_blocks(X) doubles.
  */

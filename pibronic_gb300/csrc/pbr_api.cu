@@ -53,16 +53,15 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     a.key0 = static_cast<uint32_t>(seed);
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
-    const int A2 = npair(m.A);
-    a.a2p = (A2 + 3) / 4 * 4;
-    a.qstride = m.N * m.P + 1;
+    a.rs = row_stride(m.P);
+    a.qstride = m.N * a.rs + 1;
     // threads per sample: enough that each owns <= kMaxChunk beads, more (up to a warp) when
     // the per-CTA shared memory of S = kThreads / G samples would not fit
     const int esz = m.precision == 32 ? 4 : 8;
     a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
     while (true) {
         a.S = kThreads / a.G;
-        const SmemPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.a2p, a.S, a.qstride);
+        const SmemPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride);
         if (plan.total_bytes <= kMaxSmem || a.G == 32) {
             if (plan.total_bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
             break;
@@ -120,7 +119,8 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
     a.key0 = static_cast<uint32_t>(seed);
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
-    a.qstride = m.N * m.P + 1;
+    a.rs = row_stride(m.P);
+    a.qstride = m.N * a.rs + 1;
     const size_t esz = m.precision == 32 ? sizeof(float) : sizeof(double);
     a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
     int bytes = 0;

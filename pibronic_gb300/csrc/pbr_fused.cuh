@@ -36,24 +36,33 @@ struct FusedArgs {
     uint32_t key0, key1;
     uint64_t offset;
     int G, logG, C, S;
-    int a2p;        // padded row length of the packed quadratic table in shared memory
+    int rs;         // row stride of one mode's beads in shared memory (skewed, see qidx)
     int qstride;    // elements per sample in the q region
 };
 
 __host__ __device__ inline int align_up(int x, int a) { return (x + a - 1) / a * a; }
 
+// Bead p of mode j in a sample's shared-memory block.  Beads are skewed by one slot every 32 so
+// that threads owning chunks 32 beads apart do not hit the same bank.
+__host__ __device__ __forceinline__ int qidx(int j, int p, int rs) { return j * rs + p + (p >> 5); }
+__host__ __device__ inline int row_stride(int P) { return P + ((P + 31) >> 5); }
+
+// Per-mode record of the tables read in the bead loop (one 128-bit-aligned block per mode):
+//   [0,KP) vib csch series/2 | [KP,2KP) vib tanh series/2 | [2KP,2KP+AP) vib d_a |
+//   [2KP+AP,2KP+2AP) rho d_a | 4: rho csch/2, rho tanh/2, 0, 0 | A2P: linear couplings (pairs)
+__host__ __device__ inline int rec_len(int A, int K) {
+    return 2 * align_up(K + 1, 4) + 2 * align_up(A, 4) + 4 + align_up(npair(A), 4);
+}
+
 // Shared-memory plan (in elements of the table type, esz bytes each); identical on host and device.
 struct SmemPlan {
-    int cs, th, c, d, e, l, qq, rcs, rth, rc, rd, trig, q, qlo, total_bytes;
-    __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int a2p, int S,
-                                 int qstride) {
-        const int A2 = npair(A);
-        const int N2 = npair(N);
+    int c, e, qq, rc, rec, trig, q, qlo, total_bytes;
+    __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int S, int qstride) {
+        const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        cs = take((K + 1) * N); th = take((K + 1) * N); c = take((K + 1) * A); d = take(A * N);
-        e = take(A2); l = take(N * A2); qq = take(N2 * a2p);
-        rcs = take(N); rth = take(N); rc = take(A); rd = take(A * N);
+        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
+        rec = take(N * rec_len(A, K));
         trig = take(qm == kSample ? 2 * P : 0);
         q = take(S * qstride);
         qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
@@ -63,19 +72,137 @@ struct SmemPlan {
 
 template <typename T> __device__ __forceinline__ T dev_fabs(T x) { return x < T(0) ? -x : x; }
 
+// CNT consecutive table values from shared memory, 128-bit loads where the type allows.
+template <typename T, int CNT>
+__device__ __forceinline__ void ldv(const T* __restrict__ src, T (&dst)[CNT]) {
+    if constexpr (sizeof(T) == 4 && CNT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < CNT; i += 4) {
+            const float4 v = *reinterpret_cast<const float4*>(src + i);
+            dst[i] = v.x; dst[i + 1] = v.y; dst[i + 2] = v.z; dst[i + 3] = v.w;
+        }
+    } else if constexpr (sizeof(T) == 8 && CNT % 2 == 0) {
+#pragma unroll
+        for (int i = 0; i < CNT; i += 2) {
+            const double2 v = *reinterpret_cast<const double2*>(src + i);
+            dst[i] = v.x; dst[i + 1] = v.y;
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < CNT; ++i) dst[i] = src[i];
+    }
+}
+
+// Jacobi rotation (c, s, t) annihilating a_pq of the 2x2 block [[app, apq], [apq, aqq]].
+// FP32 uses the fast reciprocal and rsqrt: any (c, s) with c^2 + s^2 = 1 keeps the sweep
+// orthogonal, an inexact angle only leaves a small a_pq for the next sweep.
+__device__ __forceinline__ void jrot(float app, float aqq, float apq, float& c, float& s, float& t) {
+    const float zeta = __fdividef(aqq - app, 2.0f * apq);
+    const float az = fabsf(zeta);
+    float tt;
+    if (az > 1e18f) {
+        tt = __fdividef(0.5f, zeta);
+    } else {
+        const float x = fmaf(zeta, zeta, 1.0f);
+        tt = copysignf(__fdividef(1.0f, az + x * rsqrtf(x)), zeta);
+    }
+    c = rsqrtf(fmaf(tt, tt, 1.0f));
+    s = tt * c;
+    t = tt;
+}
+__device__ __forceinline__ void jrot(double app, double aqq, double apq, double& c, double& s, double& t) {
+    const double zeta = (aqq - app) / (2.0 * apq);
+    const double az = fabs(zeta);
+    double tt;
+    if (az > 1e150) {
+        tt = 0.5 / zeta;
+    } else {
+        tt = 1.0 / (az + sqrt(1.0 + zeta * zeta));
+        if (zeta < 0.0) tt = -tt;
+    }
+    c = 1.0 / sqrt(1.0 + tt * tt);
+    s = tt * c;
+    t = tt;
+}
+
+// Cyclic Jacobi on symmetric a (registers) accumulating the rotations into u, which holds the
+// starting basis on entry (identity, or the previous bead's eigenvectors: a warm start).
+template <typename T, int A>
+__device__ __forceinline__ void jacobi_accumulate(T (&a)[A][A], T (&u)[A][A], int max_sweeps) {
+    if (A == 1) return;
+    const T tol = eps_of<T>::value * eps_of<T>::value;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        T off = T(0), dia = T(0);
+#pragma unroll
+        for (int p = 0; p < A; ++p) {
+            dia = fma(a[p][p], a[p][p], dia);
+#pragma unroll
+            for (int q = p + 1; q < A; ++q) off = fma(a[p][q], a[p][q], off);
+        }
+        if (off <= tol * dia || off == T(0)) break;
+#pragma unroll
+        for (int p = 0; p < A - 1; ++p) {
+#pragma unroll
+            for (int q = p + 1; q < A; ++q) {
+                const T apq = a[p][q];
+                if (apq == T(0)) continue;
+                T c, s, t;
+                jrot(a[p][p], a[q][q], apq, c, s, t);
+                a[p][p] = fma(-t, apq, a[p][p]);
+                a[q][q] = fma(t, apq, a[q][q]);
+                a[p][q] = T(0);
+                a[q][p] = T(0);
+#pragma unroll
+                for (int r = 0; r < A; ++r) {
+                    if (r == p || r == q) continue;
+                    const T arp = a[r][p], arq = a[r][q];
+                    const T np = c * arp - s * arq;
+                    const T nq = s * arp + c * arq;
+                    a[r][p] = np; a[p][r] = np;
+                    a[r][q] = nq; a[q][r] = nq;
+                }
+#pragma unroll
+                for (int r = 0; r < A; ++r) {
+                    const T urp = u[r][p], urq = u[r][q];
+                    u[r][p] = c * urp - s * urq;
+                    u[r][q] = s * urp + c * urq;
+                }
+            }
+        }
+    }
+}
+
+// Compensated (Kahan) FP32 sum for the per-chunk log accumulators; plain sum in FP64.
+template <typename T> struct LogSum;
+template <> struct LogSum<float> {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
+};
+template <> struct LogSum<double> {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
 // Phase A on the sampling path: the G threads of one sample (lanes gmask) draw the source surface
 // and the normal-mode coordinates and transform them to bead coordinates q[j][p] in shared
-// memory (row stride P).  Returns the source surface.  pimc.py:326-334, 386-389, 613-631.
+// memory (layout qidx).  Returns the source surface.  pimc.py:326-334, 386-389, 613-631.
 template <typename T>
-__device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int64_t sidx,
+__device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int rs, int64_t sidx,
                                 uint64_t offset, uint32_t key0, uint32_t key1, int g, int G, int C,
                                 int p_begin, unsigned gmask) {
     const int N = m.N, P = m.P;
     const uint64_t sg = offset + static_cast<uint64_t>(sidx);
     const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
     // source surface ~ Categorical(state weights) (pimc.py:386-389)
-    const u32x4 rs = philox4x32_10(u32x4{0xFFFFFFFFu, lo, hi, 1u}, key0, key1);
-    const float us = u01(rs.x);
+    const u32x4 rs4 = philox4x32_10(u32x4{0xFFFFFFFFu, lo, hi, 1u}, key0, key1);
+    const float us = u01(rs4.x);
     const T* cdf = static_cast<const T*>(m.src_cdf);
     int src = 0;
     for (int a = 0; a < m.A_rho - 1; ++a) src += (us >= static_cast<float>(cdf[a])) ? 1 : 0;
@@ -91,7 +218,10 @@ __device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int6
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
             const int i = 4 * cidx + t;
-            if (i < NP) qs[i] = T(z[t]) * stdp[i];
+            if (i < NP) {
+                const int j = i / P, sl = i - j * P;
+                qs[qidx(j, sl, rs)] = T(z[t]) * stdp[i];
+            }
         }
     }
     __syncwarp(gmask);
@@ -109,8 +239,11 @@ __device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int6
 #pragma unroll
             for (int jj = 0; jj < JB; ++jj) {
                 const int j = min(j0 + jj, N - 1);
-                T v = qs[j * P] * inv_sqrt_p;
-                if (even) v += ((p & 1) ? -qs[j * P + P - 1] : qs[j * P + P - 1]) * inv_sqrt_p;
+                T v = qs[qidx(j, 0, rs)] * inv_sqrt_p;
+                if (even) {
+                    const T ny = qs[qidx(j, P - 1, rs)] * inv_sqrt_p;
+                    v += (p & 1) ? -ny : ny;
+                }
                 acc[b][jj] = v;
             }
         }
@@ -122,8 +255,8 @@ __device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int6
 #pragma unroll
             for (int jj = 0; jj < JB; ++jj) {
                 const int j = min(j0 + jj, N - 1);
-                cc_c[jj] = qs[j * P + 2 * k - 1];
-                cc_s[jj] = qs[j * P + 2 * k];
+                cc_c[jj] = qs[qidx(j, 2 * k - 1, rs)];
+                cc_s[jj] = qs[qidx(j, 2 * k, rs)];
             }
 #pragma unroll
             for (int b = 0; b < kMaxChunk; ++b) {
@@ -134,7 +267,7 @@ __device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int6
                 mm[b] = mb;
                 const T cth = s_trig[2 * mb], sth = s_trig[2 * mb + 1];
 #pragma unroll
-                for (int jj = 0; jj < JB; ++jj) acc[b][jj] += cc_c[jj] * cth + cc_s[jj] * sth;
+                for (int jj = 0; jj < JB; ++jj) acc[b][jj] = fma(cc_c[jj], cth, fma(cc_s[jj], sth, acc[b][jj]));
             }
         }
         __syncwarp(gmask);
@@ -145,7 +278,7 @@ __device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int6
 #pragma unroll
                 for (int jj = 0; jj < JB; ++jj) {
                     const int j = j0 + jj;
-                    if (j < N) qs[j * P + p] = acc[b][jj] + dsrc[j];
+                    if (j < N) qs[qidx(j, p, rs)] = acc[b][jj] + dsrc[j];
                 }
             }
         }
@@ -166,21 +299,44 @@ __device__ void fill_trig(T* s_trig, int P) {
     }
 }
 
+// power-of-two renormalisation of a series matrix; returns the exponent taken out
+template <typename T, int K, int A>
+__device__ __forceinline__ int renormalise(T (&n)[K + 1][A][A]) {
+    T mx = T(0);
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(n[0][r][c]));
+    if (!(mx > T(0)) || !isfinite(mx)) return 0;
+    int e2;
+    frexp(mx, &e2);
+    const T sc = ldexp(T(1), -e2);
+#pragma unroll
+    for (int k = 0; k <= K; ++k)
+#pragma unroll
+        for (int r = 0; r < A; ++r)
+#pragma unroll
+            for (int c = 0; c < A; ++c) n[k][r][c] *= sc;
+    return e2;
+}
+
 template <int A, int K, int QM, typename T>
 __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs args) {
     constexpr int A2 = npair(A);
+    constexpr int A2P = (A2 + 3) / 4 * 4;
+    constexpr int KP = (K + 1 + 3) / 4 * 4;
+    constexpr int AP = (A + 3) / 4 * 4;
+    constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
     constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
 
     const pbr_model& m = args.m;
-    const int N = m.N, P = m.P, nfill = m.n_fill_rho;
+    const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
     const int G = args.G, C = args.C, S = args.S;
-    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, args.a2p, S, args.qstride);
-    T* s_cs = sm + plan.cs;  T* s_th = sm + plan.th;  T* s_c = sm + plan.c;  T* s_d = sm + plan.d;
-    T* s_e = sm + plan.e;    T* s_l = sm + plan.l;    T* s_qq = sm + plan.qq;
-    T* s_rcs = sm + plan.rcs; T* s_rth = sm + plan.rth; T* s_rc = sm + plan.rc; T* s_rd = sm + plan.rd;
-    T* s_trig = sm + plan.trig;
+    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, args.qstride);
+    T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
+    T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec; T* s_trig = sm + plan.trig;
 
     // ---- model tables -> shared memory (once per CTA; the grid is persistent) -----------------
     {
@@ -190,21 +346,26 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
         const T* g_qq = static_cast<const T*>(m.vib_qq);
         const T* g_rcs = static_cast<const T*>(m.rho_cs); const T* g_rth = static_cast<const T*>(m.rho_th);
         const T* g_rc = static_cast<const T*>(m.rho_c);   const T* g_rd = static_cast<const T*>(m.rho_d);
-        for (int i = threadIdx.x; i < (K + 1) * N; i += blockDim.x) { s_cs[i] = g_cs[i]; s_th[i] = g_th[i]; }
         for (int i = threadIdx.x; i < (K + 1) * A; i += blockDim.x) s_c[i] = g_c[i];
-        for (int i = threadIdx.x; i < A * N; i += blockDim.x) {
-            s_d[i] = g_d[i];
-            s_rd[i] = (i < nfill * N) ? g_rd[i] : T(0);
-        }
-        for (int i = threadIdx.x; i < A2; i += blockDim.x) s_e[i] = g_e[i];
-        for (int i = threadIdx.x; i < N * A2; i += blockDim.x) s_l[i] = g_l[i];
+        for (int i = threadIdx.x; i < A2P; i += blockDim.x) s_e[i] = (i < A2) ? g_e[i] : T(0);
         const int N2 = npair(N);
-        for (int i = threadIdx.x; i < N2 * args.a2p; i += blockDim.x) {
-            const int row = i / args.a2p, col = i - row * args.a2p;
+        for (int i = threadIdx.x; i < N2 * A2P; i += blockDim.x) {
+            const int row = i / A2P, col = i - row * A2P;
             s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
         }
-        for (int i = threadIdx.x; i < N; i += blockDim.x) { s_rcs[i] = g_rcs[i]; s_rth[i] = g_rth[i]; }
         for (int i = threadIdx.x; i < A; i += blockDim.x) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
+        for (int i = threadIdx.x; i < N * MR; i += blockDim.x) {
+            const int j = i / MR, o = i - j * MR;
+            T v = T(0);
+            if (o < KP) { if (o <= K) v = g_cs[o * N + j]; }
+            else if (o < 2 * KP) { if (o - KP <= K) v = g_th[(o - KP) * N + j]; }
+            else if (o < 2 * KP + AP) { const int a = o - 2 * KP; if (a < A) v = g_d[a * N + j]; }
+            else if (o < 2 * KP + 2 * AP) { const int a = o - 2 * KP - AP; if (a < nfill) v = g_rd[a * N + j]; }
+            else if (o == 2 * KP + 2 * AP) v = g_rcs[j];
+            else if (o == 2 * KP + 2 * AP + 1) v = g_rth[j];
+            else if (o >= 2 * KP + 2 * AP + 4) { const int pr = o - 2 * KP - 2 * AP - 4; if (pr < A2) v = g_l[j * A2 + pr]; }
+            s_rec[i] = v;
+        }
         if (QM == kSample) fill_trig<T>(s_trig, P);
     }
     __syncthreads();
@@ -227,28 +388,33 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 
         // ============================ phase A: q into shared memory ============================
         if (active) {
+            const int NP = N * P;
             if (QM == kSample) {
-                const int src = draw_sample_smem<T>(m, s_trig, qs, sidx, args.offset, args.key0,
+                const int src = draw_sample_smem<T>(m, s_trig, qs, rs, sidx, args.offset, args.key0,
                                                     args.key1, g, G, C, p_begin, gmask);
                 if (args.out.src_out && g == 0) args.out.src_out[sidx] = src;
                 if (args.out.q_out) {
-                    const int NP = N * P;
                     float* qo = args.out.q_out + sidx * static_cast<int64_t>(NP);
-                    for (int i = g; i < NP; i += G) qo[i] = static_cast<float>(qs[i]);
-                }
-            } else {
-                const int NP = N * P;
-                if (QM == kQ64) {
-                    const double* qin = static_cast<const double*>(args.q_in) + sidx * static_cast<int64_t>(NP);
                     for (int i = g; i < NP; i += G) {
-                        const double v = qin[i];
-                        const T hi = T(v);
-                        qs[i] = hi;
-                        if (kLo) ql[i] = T(v - static_cast<double>(hi));
+                        const int j = i / P, p = i - j * P;
+                        qo[i] = static_cast<float>(qs[qidx(j, p, rs)]);
                     }
-                } else {
-                    const float* qin = static_cast<const float*>(args.q_in) + sidx * static_cast<int64_t>(NP);
-                    for (int i = g; i < NP; i += G) qs[i] = T(qin[i]);
+                }
+            } else if (QM == kQ64) {
+                const double* qin = static_cast<const double*>(args.q_in) + sidx * static_cast<int64_t>(NP);
+                for (int i = g; i < NP; i += G) {
+                    const int j = i / P, p = i - j * P;
+                    const double v = qin[i];
+                    const T hi = T(v);
+                    qs[qidx(j, p, rs)] = hi;
+                    if (kLo) ql[qidx(j, p, rs)] = T(v - static_cast<double>(hi));
+                }
+                __syncwarp(gmask);
+            } else {
+                const float* qin = static_cast<const float*>(args.q_in) + sidx * static_cast<int64_t>(NP);
+                for (int i = g; i < NP; i += G) {
+                    const int j = i / P, p = i - j * P;
+                    qs[qidx(j, p, rs)] = T(qin[i]);
                 }
                 __syncwarp(gmask);
             }
@@ -263,51 +429,56 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                 for (int c = 0; c < A; ++c) nser[k][r][c] = (k == 0 && r == c) ? T(1) : T(0);
         int nexp = 0;
-        double lrho[A];
-#pragma unroll
-        for (int a = 0; a < A; ++a) lrho[a] = 0.0;
-        double lsum = 0.0;
-        bool first = true;
+        LogSum<T> lrho[A];
+        LogSum<T> lsum;
+        T uw[A][A];          // eigenvectors of the previous bead: warm start of the next Jacobi
 
         if (active) {
             for (int p = p_begin; p < p_end; ++p) {
                 const int pn = (p + 1 == P) ? 0 : p + 1;
+                const int ip = qidx(0, p, rs), ipn = qidx(0, pn, rs);
                 // ---- O-matrix exponents and the linear part of V, one pass over the modes ----
-                T phv[K + 1][A], phr[A], v[A2];
+                T phv[K + 1][A], phr[A], v[A2P];
 #pragma unroll
                 for (int k = 0; k <= K; ++k)
 #pragma unroll
                     for (int a = 0; a < A; ++a) phv[k][a] = s_c[k * A + a];
 #pragma unroll
                 for (int a = 0; a < A; ++a) phr[a] = s_rc[a];
-#pragma unroll
-                for (int pr = 0; pr < A2; ++pr) v[pr] = s_e[pr];
+                ldv(s_e, v);
                 T dsum[K + 1];
 #pragma unroll
                 for (int k = 0; k <= K; ++k) dsum[k] = T(0);
                 T rdsum = T(0);
                 for (int j = 0; j < N; ++j) {
-                    const T qa = qs[j * P + p], qb = qs[j * P + pn];
+                    const T* rec = s_rec + j * MR;
+                    T cs[KP], th[KP], dv[AP], rdv[AP], rx[4], lr[A2P];
+                    ldv(rec, cs);
+                    ldv(rec + KP, th);
+                    ldv(rec + 2 * KP, dv);
+                    ldv(rec + 2 * KP + AP, rdv);
+                    ldv(rec + 2 * KP + 2 * AP, rx);
+                    ldv(rec + 2 * KP + 2 * AP + 4, lr);
+                    const T qa = qs[ip + j * rs], qb = qs[ipn + j * rs];
                     T dq = qa - qb;
-                    if (kLo) dq += ql[j * P + p] - ql[j * P + pn];
+                    if (kLo) dq += ql[ip + j * rs] - ql[ipn + j * rs];
                     const T dq2 = dq * dq;
 #pragma unroll
-                    for (int k = 0; k <= K; ++k) dsum[k] = fma(s_cs[k * N + j], dq2, dsum[k]);
-                    rdsum = fma(s_rcs[j], dq2, rdsum);
+                    for (int k = 0; k <= K; ++k) dsum[k] = fma(cs[k], dq2, dsum[k]);
+                    rdsum = fma(rx[0], dq2, rdsum);
 #pragma unroll
                     for (int a = 0; a < A; ++a) {
-                        const T da = s_d[a * N + j];
-                        const T ua = qa - da, ub = qb - da;
+                        const T ua = qa - dv[a], ub = qb - dv[a];
                         const T sq = fma(ua, ua, ub * ub);
 #pragma unroll
-                        for (int k = 0; k <= K; ++k) phv[k][a] = fma(-s_th[k * N + j], sq, phv[k][a]);
+                        for (int k = 0; k <= K; ++k) phv[k][a] = fma(-th[k], sq, phv[k][a]);
                         if (a < nfill) {
-                            const T ra = qa - s_rd[a * N + j], rb = qb - s_rd[a * N + j];
-                            phr[a] = fma(-s_rth[j], fma(ra, ra, rb * rb), phr[a]);
+                            const T ra = qa - rdv[a], rb = qb - rdv[a];
+                            phr[a] = fma(-rx[1], fma(ra, ra, rb * rb), phr[a]);
                         }
                     }
 #pragma unroll
-                    for (int pr = 0; pr < A2; ++pr) v[pr] = fma(s_l[j * A2 + pr], qa, v[pr]);
+                    for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
                 }
 #pragma unroll
                 for (int a = 0; a < A; ++a) {
@@ -322,10 +493,10 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                 for (int a = 0; a < A; ++a)
                     if (a < nfill) lmax = max(lmax, phr[a]);
-                lsum += static_cast<double>(lmax);
+                lsum.add(lmax);
 #pragma unroll
                 for (int a = 0; a < A; ++a)
-                    if (a < nfill) lrho[a] += static_cast<double>(phr[a] - lmax);
+                    if (a < nfill) lrho[a].add(phr[a] - lmax);
                 T osr[K + 1][A];
 #pragma unroll
                 for (int a = 0; a < A; ++a) {
@@ -336,7 +507,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                         T acc = T(0);
 #pragma unroll
                         for (int i = 1; i <= k; ++i) acc = fma(T(i) * phv[i][a], ek[k - i], acc);
-                        ek[k] = acc / T(k);
+                        ek[k] = acc * (T(1) / T(k));
                     }
                     const T e0 = dev_exp<T>(phv[0][a] - lmax);
 #pragma unroll
@@ -346,24 +517,55 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                 {
                     int row = 0;
                     for (int d = 0; d < N; ++d) {
-                        const T qd = qs[d * P + p];
+                        const T qd = qs[ip + d * rs];
                         for (int e = 0; e <= d; ++e, ++row) {
-                            const T w = qd * qs[e * P + p];
-                            const T* qrow = s_qq + row * args.a2p;
+                            const T w = qd * qs[ip + e * rs];
+                            T qrow[A2P];
+                            ldv(s_qq + row * A2P, qrow);
 #pragma unroll
                             for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
                         }
                     }
                 }
-                // ---- M = exp(-tau V) by Jacobi ----
+                // ---- M = exp(-tau V) by Jacobi, warm-started from the previous bead ----
                 T M[A][A];
                 {
-                    T am[A][A], u[A][A];
+                    const bool cold = ((p - p_begin) & 7) == 0;   // fresh basis every 8 beads
+                    if (cold) {
+#pragma unroll
+                        for (int r = 0; r < A; ++r)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) uw[r][c] = (r == c) ? T(1) : T(0);
+                    }
+                    T am[A][A];
 #pragma unroll
                     for (int b = 0; b < A; ++b)
 #pragma unroll
                         for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
-                    jacobi_eigh<T, A>(am, u, sizeof(T) == 4 ? 10 : 16);
+                    if (!cold) {
+                        // am <- U^T V U in the previous bead's eigenbasis
+                        T w[A][A];
+#pragma unroll
+                        for (int r = 0; r < A; ++r)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int mm = 0; mm < A; ++mm) acc = fma(am[r][mm], uw[mm][c], acc);
+                                w[r][c] = acc;
+                            }
+#pragma unroll
+                        for (int r = 0; r < A; ++r)
+#pragma unroll
+                            for (int c = 0; c <= r; ++c) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int mm = 0; mm < A; ++mm) acc = fma(uw[mm][r], w[mm][c], acc);
+                                am[r][c] = acc;
+                                am[c][r] = acc;
+                            }
+                    }
+                    jacobi_accumulate<T, A>(am, uw, sizeof(T) == 4 ? 10 : 16);
                     T t[A];
                     T tmax = -tau_l2 * am[0][0];
 #pragma unroll
@@ -379,20 +581,19 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                         for (int c = 0; c <= r; ++c) {
                             T acc = T(0);
 #pragma unroll
-                            for (int i = 0; i < A; ++i) acc = fma(u[r][i] * ev[i], u[c][i], acc);
+                            for (int i = 0; i < A; ++i) acc = fma(uw[r][i] * ev[i], uw[c][i], acc);
                             M[r][c] = acc;
                             M[c][r] = acc;
                         }
                 }
                 // ---- ring update N(h) <- N(h) M diag(O(h)) ----
-                if (first) {
+                if (p == p_begin) {
 #pragma unroll
                     for (int k = 0; k <= K; ++k)
 #pragma unroll
                         for (int r = 0; r < A; ++r)
 #pragma unroll
                             for (int c = 0; c < A; ++c) nser[k][r][c] = M[r][c] * osr[k][c];
-                    first = false;
                 } else {
 #pragma unroll
                     for (int r = 0; r < A; ++r) {
@@ -417,30 +618,15 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                             }
                     }
                 }
-                // ---- power-of-two renormalisation ----
-                {
-                    T mx = T(0);
-#pragma unroll
-                    for (int r = 0; r < A; ++r)
-#pragma unroll
-                        for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nser[0][r][c]));
-                    if (mx > T(0) && isfinite(mx)) {
-                        int e2;
-                        frexp(mx, &e2);
-                        const T sc = ldexp(T(1), -e2);
-                        nexp += e2;
-#pragma unroll
-                        for (int k = 0; k <= K; ++k)
-#pragma unroll
-                            for (int r = 0; r < A; ++r)
-#pragma unroll
-                                for (int c = 0; c < A; ++c) nser[k][r][c] *= sc;
-                    }
-                }
+                nexp += renormalise<T, K, A>(nser);
             }
         }
 
         // ============================ phase C: combine the chunks ===============================
+        double lr_d[A];
+#pragma unroll
+        for (int a = 0; a < A; ++a) lr_d[a] = lrho[a].value();
+        double ls_d = lsum.value();
         for (int st = 1; st < G; st <<= 1) {
             T oth[K + 1][A][A];
 #pragma unroll
@@ -471,29 +657,13 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                         for (int c = 0; c < A; ++c) nser[k][r][c] = z[k][c];
                 }
                 nexp += oexp;
-                T mx = T(0);
-#pragma unroll
-                for (int r = 0; r < A; ++r)
-#pragma unroll
-                    for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nser[0][r][c]));
-                if (mx > T(0) && isfinite(mx)) {
-                    int e2;
-                    frexp(mx, &e2);
-                    const T sc = ldexp(T(1), -e2);
-                    nexp += e2;
-#pragma unroll
-                    for (int k = 0; k <= K; ++k)
-#pragma unroll
-                        for (int r = 0; r < A; ++r)
-#pragma unroll
-                            for (int c = 0; c < A; ++c) nser[k][r][c] *= sc;
-                }
+                nexp += renormalise<T, K, A>(nser);
             }
         }
         for (int st = G >> 1; st >= 1; st >>= 1) {
 #pragma unroll
-            for (int a = 0; a < A; ++a) lrho[a] += __shfl_down_sync(0xffffffffu, lrho[a], st, G);
-            lsum += __shfl_down_sync(0xffffffffu, lsum, st, G);
+            for (int a = 0; a < A; ++a) lr_d[a] += __shfl_down_sync(0xffffffffu, lr_d[a], st, G);
+            ls_d += __shfl_down_sync(0xffffffffu, ls_d, st, G);
         }
 
         // ============================ phase D: outputs ==========================================
@@ -509,7 +679,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
             double rho = 0.0;
 #pragma unroll
             for (int a = 0; a < A; ++a)
-                if (a < nfill) rho += exp(lrho[a]);
+                if (a < nfill) rho += exp(lr_d[a]);
             const pbr_outputs& o = args.out;
             o.s_rho[sidx] = rho;
             o.s_g[sidx] = coef[0];
@@ -527,7 +697,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                 for (int k = 0; k <= K; ++k) o.g_coef[sidx * (K + 1) + k] = coef[k];
             }
-            if (o.log_scale) o.log_scale[sidx] = lsum + static_cast<double>(P) * m.log_c0;
+            if (o.log_scale) o.log_scale[sidx] = ls_d + static_cast<double>(P) * m.log_c0;
             if (bad) flag_status(o.status, PBR_ERR_NONFINITE);
         }
         __syncwarp();
@@ -541,7 +711,7 @@ __global__ void __launch_bounds__(kThreads) sample_q_kernel(const FusedArgs args
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* s_trig = reinterpret_cast<T*>(smem_raw);
     const pbr_model& m = args.m;
-    const int N = m.N, P = m.P, G = args.G, C = args.C, S = args.S;
+    const int N = m.N, P = m.P, G = args.G, C = args.C, S = args.S, rs = args.rs;
     fill_trig<T>(s_trig, P);
     __syncthreads();
     const int tid = threadIdx.x, grp = tid >> args.logG, g = tid & (G - 1), lane = tid & 31;
@@ -551,12 +721,15 @@ __global__ void __launch_bounds__(kThreads) sample_q_kernel(const FusedArgs args
          base += static_cast<int64_t>(gridDim.x) * S) {
         const int64_t sidx = base + grp;
         if (sidx < args.X) {
-            const int src = draw_sample_smem<T>(m, s_trig, qs, sidx, args.offset, args.key0,
+            const int src = draw_sample_smem<T>(m, s_trig, qs, rs, sidx, args.offset, args.key0,
                                                 args.key1, g, G, C, g * C, gmask);
             if (args.out.src_out && g == 0) args.out.src_out[sidx] = src;
             const int NP = N * P;
             float* qo = args.out.q_out + sidx * static_cast<int64_t>(NP);
-            for (int i = g; i < NP; i += G) qo[i] = static_cast<float>(qs[i]);
+            for (int i = g; i < NP; i += G) {
+                const int j = i / P, p = i - j * P;
+                qo[i] = static_cast<float>(qs[qidx(j, p, rs)]);
+            }
         }
         __syncwarp();
     }

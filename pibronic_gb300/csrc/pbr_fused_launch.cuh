@@ -9,8 +9,8 @@ namespace pbr {
 
 template <int A, int K, int QM, typename T>
 static int launch_fused_one(const FusedArgs& args, cudaStream_t stream) {
-    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.a2p,
-                        args.S, args.qstride);
+    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S,
+                        args.qstride);
     auto kern = pimc_fused_kernel<A, K, QM, T>;
     static int configured = 0;    // dynamic shared memory opt-in already granted to this kernel
     if (plan.total_bytes > 48 * 1024 && plan.total_bytes > configured) {

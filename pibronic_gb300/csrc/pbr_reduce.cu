@@ -107,9 +107,11 @@ __global__ void jackknife_partial(const double* rho, const double* g, const doub
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double r, s1, s2;
         terms(rho, g, gp, gm, i, db, r, s1, s2);
+        // f_E,i - E0 and f_C,i - C0 written without the cancellation of the direct differences:
+        //   (S - x_i)/(S_r - r_i) - S/S_r = -(S_r x_i - S r_i) / (S_r (S_r - r_i))
         const double den = Sr * (Sr - r);
-        const double dE = -(Sr * s1 - S1 * r) / den;          // f_E,i - E0
-        const double dC = ((Sr * s2 - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2;
+        const double dE = (Sr * s1 - S1 * r) / den;
+        const double dC = (-(Sr * s2 - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2;
         push(m[0], dE);
         push(m[1], dC);
     }

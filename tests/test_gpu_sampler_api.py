@@ -250,6 +250,7 @@ def test_errors_are_reported_not_faulted(tmp_path):
     q[3, 1, 5] = float("nan")
     out = evaluate_device(data.plan, 16, q=q)
     assert int(out["status"].item()) == _native.PBR_ERR_NONFINITE
+    (tmp_path / "big").mkdir()
     FS2, data2 = make_box(tmp_path / "big", A=2, N=3, P=300, X=16)
     with pytest.raises(AssertionError):
         evaluate_device(data2.plan, 16, seed=1)        # sampling path supports P <= 256
