@@ -23,6 +23,7 @@ extern "C" {
 #define PBR_ERR_CUDA        2   /* a CUDA launch or runtime call failed                      */
 #define PBR_ERR_UNSUPPORTED 3   /* no compiled variant for these sizes                       */
 #define PBR_ERR_NONFINITE   4   /* a kernel produced a non-finite value (per-sample flag)   */
+#define PBR_ERR_CAPACITY    5   /* request exceeds a fixed capacity of the library           */
 
 /* ---- limits of the fused kernels ---------------------------------------------------------- */
 #define PBR_MAX_A      8        /* surfaces of the coupled model                            */
@@ -203,6 +204,25 @@ int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s
 
 /* Number of partial blocks the reductions use for X samples. */
 int64_t pbr_reduce_blocks(int64_t X);
+
+/*
+ * pbr_reduce_terms without a scratch argument: allocates nothing and takes no scratch buffer.
+ * No counterpart in the reference.  It is for callers that cannot allocate device memory -- a
+ * plain FFI caller with no GPU array library to allocate through, or one whose device memory is
+ * held by its own pool and that must not call cudaMalloc/cudaFree (they can synchronize the
+ * device).  The partial sums live in a fixed file-scope device array of 9 * 1024 doubles
+ * (72 KiB) that every device loading the library keeps until the process exits, so
+ * X <= pbr_reduce_terms_static_max_samples() = 4,194,304; larger X returns PBR_ERR_CAPACITY and
+ * launches nothing.  Results equal pbr_reduce_terms's for the same inputs.  The first call on a
+ * device looks the array's device address up (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be serialised by the
+ * caller.
+ */
+int pbr_reduce_terms_static(const double* s_rho, const double* s_g, const double* s_gp,
+                            const double* s_gm, int64_t X, double delta_beta, double* moments,
+                            void* stream);
+int64_t pbr_reduce_terms_static_max_samples(void);
 
 /*
  * FP32 FMA throughput probe: blocks x 256 threads, each running 8 independent FMA chains for

@@ -13,11 +13,13 @@ _LOCK = threading.Lock()
 _LIB = None
 
 PBR_OK, PBR_ERR_ARG, PBR_ERR_CUDA, PBR_ERR_UNSUPPORTED, PBR_ERR_NONFINITE = 0, 1, 2, 3, 4
+PBR_ERR_CAPACITY = 5
 _STATUS_TEXT = {
     PBR_ERR_ARG: "invalid argument",
     PBR_ERR_CUDA: "CUDA error",
     PBR_ERR_UNSUPPORTED: "unsupported sizes for the compiled kernels",
     PBR_ERR_NONFINITE: "non-finite result",
+    PBR_ERR_CAPACITY: "request exceeds a fixed capacity of the library",
 }
 
 #: every symbol declared in include/pibronic_gb300.h
@@ -26,7 +28,7 @@ EXPORTED = (
     "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_divide_o_matrix", "pbr_denominator",
     "pbr_coupling_eigh", "pbr_numerator",
     "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_fma_probe",
-    "pbr_version",
+    "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples", "pbr_version",
 )
 
 
@@ -75,6 +77,8 @@ def _declare(lib):
         "pbr_reduce_jackknife": (C.c_int, [vp, vp, vp, vp, i64, f64, f64, vp, vp, vp, vp]),
         "pbr_reduce_blocks": (i64, [i64]),
         "pbr_fma_probe": (C.c_int, [vp, i32, i32, C.POINTER(f64), vp]),
+        "pbr_reduce_terms_static": (C.c_int, [vp, vp, vp, vp, i64, f64, vp, vp]),
+        "pbr_reduce_terms_static_max_samples": (i64, []),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

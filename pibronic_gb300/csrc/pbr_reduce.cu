@@ -184,3 +184,69 @@ int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free variant of pbr_reduce_terms.
+//
+// For callers that cannot allocate device memory: a plain FFI caller (ctypes from a job script,
+// say) that has no GPU array library to allocate through, or a caller whose device memory is
+// held by its own pool and that must not call cudaMalloc / cudaFree, which can synchronize the
+// device.  The partial-sum scratch lives in this file-scope array instead of a caller buffer.
+// Every device that loads the library keeps the array (kStaticScratchDoubles doubles, 72 KiB)
+// until the process exits.
+// ---------------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr int kStaticBlocks = 1024;                                 // partial blocks held
+constexpr int64_t kStaticMaxSamples = static_cast<int64_t>(kStaticBlocks) * kPerBlock;
+constexpr int kStaticScratchDoubles = 9 * kStaticBlocks;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
+
+std::mutex g_static_mutex;
+double* g_static_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_static_scratch on the current device, looked up once per device.  In
+// host code the symbol name is only a host-side stand-in for the array, so kernels must be given
+// this address, never &g_static_scratch.
+int static_scratch_address(double** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PBR_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (g_static_addr[dev] == nullptr) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_static_scratch) != cudaSuccess || p == nullptr)
+            return PBR_ERR_CUDA;
+        g_static_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_static_addr[dev];
+    return PBR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t pbr_reduce_terms_static_max_samples(void) { return kStaticMaxSamples; }
+
+int pbr_reduce_terms_static(const double* s_rho, const double* s_g, const double* s_gp,
+                            const double* s_gm, int64_t X, double delta_beta, double* moments,
+                            void* stream) {
+    if (!s_rho || !s_g || !moments || X < 1) return PBR_ERR_ARG;
+    if ((s_gp == nullptr) != (s_gm == nullptr)) return PBR_ERR_ARG;
+    if (X > kStaticMaxSamples) return PBR_ERR_CAPACITY;
+    double* scratch = nullptr;
+    const int rc = static_scratch_address(&scratch);
+    if (rc != PBR_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int nb = nblocks_for(X);          // <= kStaticBlocks for X <= kStaticMaxSamples
+    // every partial slot the merge reads is written by terms_partial first: nothing to clear
+    terms_partial<<<nb, kRedThreads, 0, st>>>(s_rho, s_g, s_gp, s_gm, X, delta_beta, scratch);
+    final_merge<3><<<1, kRedThreads, 0, st>>>(scratch, nb, moments);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+}  // extern "C"
