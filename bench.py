@@ -257,7 +257,8 @@ def run_ours(args):
     data.blocks = X // data.block_size
     data.seed = 0x5EED + rank
     data.preprocess()
-    plan = data.plan
+    from pibronic_gb300.plan import DevicePlan
+    plan = DevicePlan(data.prepared, precision=32, variant=args.variant) if args.variant else data.plan
     stream = torch.cuda.current_stream()
     dev = torch.device("cuda", local)
     bufs = {k: torch.empty(X, dtype=torch.float64, device=dev) for k in ("s_rho", "s_g", "s_gp", "s_gm")}
@@ -403,6 +404,7 @@ def main():
     ap.add_argument("--samples", type=int, default=1_000_000, help="samples per step per GPU")
     ap.add_argument("--cpu-samples", type=int, default=400, help="samples per host process (CPU legs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variant", type=int, default=0, help="fused-kernel form: 0 auto, 1 chunks, 2 teams")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -26,7 +26,7 @@ extern "C" {
 #define PBR_ERR_CAPACITY    5   /* request exceeds a fixed capacity of the library           */
 
 /* ---- limits of the fused kernels ---------------------------------------------------------- */
-#define PBR_MAX_A      8        /* surfaces of the coupled model                            */
+#define PBR_MAX_A      8        /* surfaces of the coupled model (fused kernels)            */
 #define PBR_MAX_A_RHO  16       /* surfaces of the sampling model                            */
 #define PBR_MAX_N      64       /* modes                                                    */
 #define PBR_MAX_P      1024     /* beads                                                    */
@@ -48,11 +48,12 @@ extern "C" {
  *   vib_l    [N * A(A+1)/2]     linear couplings, diagonal folded away (pimc.py:214)
  *   vib_qq   [N(N+1)/2 * A(A+1)/2]  for mode pair (d>=e): 1/2 (Q_de + Q_ed) if d>e, 1/2 Q_dd if d==e
  *   rho_cs, rho_th [N], rho_c [A_rho], rho_d [A_rho * N]   the sampling model at beta (order 0)
- *   mode_std [A_rho * N * P]    1/sqrt(2 coth_aj - csch_aj lambda_s) for ring normal mode s in
- *                               the real Fourier order: s=0 constant, s=2k-1 / 2k the cos / sin
- *                               pair of frequency k, s=P-1 the alternating mode when P is even
- *                               (pimc.py:402-404; any orthonormal eigenbasis of the ring gives
- *                               the same distribution of q)
+ *   ring_chol [3 * N * P]       per mode j, the bead precision of rho, 2 coth_j I - csch_j C
+ *                               (C the ring adjacency; pimc.py:402-404), factored L L^T: a_p =
+ *                               1/L_pp, b_p = L_{p+1,p} (L_{P-1,P-2} at p = P-2), c_p = L_{P-1,p}
+ *                               (p <= P-3), as arrays a[j][p], b[j][p], c[j][p].  The matrix is
+ *                               cyclic tridiagonal, so L is bidiagonal plus a dense last row and
+ *                               q - d = L^-T z (z standard normal) costs O(P) per mode.
  *   src_cdf  [A_rho]            cumulative normalised state weights       (pimc.py:343-350)
  *
  * The bead coordinates are x_pa = q_p - d_a and the O-matrix exponent is evaluated in the
@@ -62,7 +63,8 @@ extern "C" {
 typedef struct pbr_model {
     int32_t A, A_rho, n_fill_rho, N, P, K;
     int32_t precision;          /* 32 or 64: element type of every table below               */
-    int32_t pad0;
+    int32_t variant;            /* fused-kernel form: 0 auto, 1 register chunks (A <= 4),
+                                   2 bead-parallel + row teams (A <= 8)                       */
     double  tau;                /* central beta / P; M = exp(-tau V) always uses it          */
     double  delta_beta;         /* beta step of the finite differences g(beta +- db)         */
     double  log_c0;             /* common offset removed from vib_c and rho_c at order 0     */
@@ -77,7 +79,7 @@ typedef struct pbr_model {
     const void* rho_th;
     const void* rho_c;
     const void* rho_d;
-    const void* mode_std;
+    const void* ring_chol;
     const void* src_cdf;
 } pbr_model;
 
@@ -103,7 +105,8 @@ typedef struct pbr_outputs {
 
 /*
  * Fused block evaluation with on-device sampling: draws X samples (Philox4x32-10 keyed by
- * seed, counter = offset + sample index), builds the O matrices of rho and of the coupled model
+ * seed, counter = offset + sample index; the source surface from the state weights, then for each
+ * mode q - d_src = L^-T z by back substitution), builds the O matrices of rho and of the coupled model
  * and its beta series, S12 scaling, V(q), Jacobi eigensolver, M = exp(-tau V), the ring product
  * with power-of-two log-scaling, and the traces.
  * Replaces one pass of the block loop of block_compute_pm / block_compute
@@ -231,6 +234,78 @@ int64_t pbr_reduce_terms_static_max_samples(void);
  * (a measurement utility).
  */
 int pbr_fma_probe(float* out, int32_t blocks, int32_t iters, double* flops, void* stream);
+
+/* ============================================================================================
+ * Learned importance proposal (affine-coupling flow over whitened ring normal modes).
+ * No counterpart in the reference: Pibronic's learned-proposal seam only produces training data
+ * (block_compute_gR*, pimc.py:1216-1338); these kernels train and apply the proposal on the GPU.
+ * All arrays are FP32 unless stated, row-major, device pointers.
+ * ============================================================================================ */
+
+/* One coupling layer: D coordinates split into I conditioning (idx_a) and J transformed (idx_b)
+ * positions; conditioner tanh(tanh(y_A W1 + b1) W2 + b2) W3 + b3 with W1 [I][H], W2 [H][H],
+ * W3 [H][2J] (the first J outputs give s = 2 tanh(raw/2), the last J give t). */
+typedef struct pbr_flow_layer {
+    int32_t D, I, J, H;
+    const int32_t* idx_a;
+    const int32_t* idx_b;
+    const float* W1; const float* b1;
+    const float* W2; const float* b2;
+    const float* W3; const float* b3;
+} pbr_flow_layer;
+
+/* Activations a training pass keeps per layer: ya [X][I], h1 / h2 [X][H], s / yb [X][J]. */
+typedef struct pbr_flow_save {
+    float* ya; float* h1; float* h2; float* s; float* yb;
+} pbr_flow_save;
+
+/* y [X][N*nsel] = whitened ring normal-mode slots s < nsel of q - center (center [N] FP64,
+ * inv_sigma [N*nsel] FP64 = sqrt(2 coth - csch lambda_s)); U [X] (FP64) = the rest of rho's
+ * bead quadratic form sum_j (q_j - c_j)^T Lambda_j (q_j - c_j) - |y|^2 (rho_csch [N],
+ * rho_tanh2 [N] = tanh(tau w / 2), FP64).  nsel <= 8. */
+int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t nsel, const double* center,
+                     const double* inv_sigma, const double* rho_csch, const double* rho_tanh2, float* y,
+                     double* U, void* stream);
+
+/* x = q + sum_{s<nsel} B_ps sigma_js (y_new - y)_js  (sigma [N*nsel] FP64). */
+int pbr_flow_apply(const float* q, const float* y, const float* y_new, int64_t X, int32_t N, int32_t P,
+                   int32_t nsel, const double* sigma, float* x, void* stream);
+
+/* One coupling layer in place on y [X][D]; direction +1 (sampling: y_B e^s + t, logdet += sum s)
+ * or -1 (density: (y_B - t) e^-s, logdet -= sum s); logdet [X] FP64; save nullable. */
+int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64_t X, float* y,
+                           double* logdet, const pbr_flow_save* save, void* stream);
+
+/* Back-propagation through one layer of the -1 direction using its saved activations:
+ * gy [X][D] holds dL/d(output) on entry, dL/d(input) on exit; rt [X] the per-sample weights of
+ * the log-det term; writes g_o [X][2J], g_z2 [X][H], g_z1 [X][H] for the weight gradients. */
+int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, const float* rt,
+                            const pbr_flow_save* save, float* g_o, float* g_z2, float* g_z1, void* stream);
+
+/* C [M][N] = beta C + sum_x A[x][M] B[x][N], split over the batch and reduced in a fixed order;
+ * scratch holds pbr_gemm_tn_scratch(X, M, N) floats. */
+int pbr_gemm_tn_acc(const float* A, const float* B, int64_t X, int32_t M, int32_t N, float beta, float* C,
+                    float* scratch, void* stream);
+int64_t pbr_gemm_tn_scratch(int64_t X, int32_t M, int32_t N);
+
+/* out [N] = column sums of B [X][N]. */
+int pbr_colsum(const float* B, int64_t X, int32_t N, float* out, void* stream);
+
+/* Base mixture on y0 [X][D]: lse [X] (FP64, nullable) = log sum_a exp(log_pi_a - |y0 - mu_a|^2/2);
+ * with rt: gy [X][D] = rt sum_a gamma_a (y0 - mu_a), rgam [X][A] = rt gamma, lossterm [X] (FP64)
+ * = -rt (lse + ld) (ld [X] FP64).  Outputs nullable.  A <= 16. */
+int pbr_flow_base(const float* y0, const double* ld, int64_t X, int32_t D, int32_t A, const float* mu,
+                  const float* log_pi, const float* rt, float* gy, float* rgam, double* lossterm,
+                  double* lse, void* stream);
+
+/* s_q [X] = exp(lse_y - U/2 - logdet - log_scale_x) (all FP64): the proposal density of the
+ * flowed sample in the scale of its PIMC outputs (pbr_outputs.log_scale). */
+int pbr_flow_weights(const double* lse_y, const double* U, const double* logdet, const double* log_scale_x,
+                     int64_t X, double* s_q, void* stream);
+
+/* Adam step (bias-corrected with the 1-based step). */
+int pbr_adam(float* param, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
+             float beta2, float eps, int32_t step, void* stream);
 
 /* Library version string and the SM architecture it was built for. */
 const char* pbr_version(void);

@@ -28,7 +28,10 @@ EXPORTED = (
     "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_divide_o_matrix", "pbr_denominator",
     "pbr_coupling_eigh", "pbr_numerator",
     "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_fma_probe",
-    "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples", "pbr_version",
+    "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples",
+    "pbr_flow_prepare", "pbr_flow_apply", "pbr_flow_layer_forward", "pbr_flow_layer_backward",
+    "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
+    "pbr_adam", "pbr_version",
 )
 
 
@@ -36,14 +39,27 @@ class PbrModel(C.Structure):
     """Mirror of ``pbr_model``."""
     _fields_ = [
         ("A", C.c_int32), ("A_rho", C.c_int32), ("n_fill_rho", C.c_int32), ("N", C.c_int32),
-        ("P", C.c_int32), ("K", C.c_int32), ("precision", C.c_int32), ("pad0", C.c_int32),
+        ("P", C.c_int32), ("K", C.c_int32), ("precision", C.c_int32), ("variant", C.c_int32),
         ("tau", C.c_double), ("delta_beta", C.c_double), ("log_c0", C.c_double),
         ("vib_cs", C.c_void_p), ("vib_th", C.c_void_p), ("vib_c", C.c_void_p),
         ("vib_d", C.c_void_p), ("vib_e", C.c_void_p), ("vib_l", C.c_void_p),
         ("vib_qq", C.c_void_p), ("rho_cs", C.c_void_p), ("rho_th", C.c_void_p),
-        ("rho_c", C.c_void_p), ("rho_d", C.c_void_p), ("mode_std", C.c_void_p),
+        ("rho_c", C.c_void_p), ("rho_d", C.c_void_p), ("ring_chol", C.c_void_p),
         ("src_cdf", C.c_void_p),
     ]
+
+
+class PbrFlowLayer(C.Structure):
+    """Mirror of ``pbr_flow_layer``."""
+    _fields_ = [("D", C.c_int32), ("I", C.c_int32), ("J", C.c_int32), ("H", C.c_int32),
+                ("idx_a", C.c_void_p), ("idx_b", C.c_void_p), ("W1", C.c_void_p), ("b1", C.c_void_p),
+                ("W2", C.c_void_p), ("b2", C.c_void_p), ("W3", C.c_void_p), ("b3", C.c_void_p)]
+
+
+class PbrFlowSave(C.Structure):
+    """Mirror of ``pbr_flow_save``."""
+    _fields_ = [("ya", C.c_void_p), ("h1", C.c_void_p), ("h2", C.c_void_p), ("s", C.c_void_p),
+                ("yb", C.c_void_p)]
 
 
 class PbrOutputs(C.Structure):
@@ -79,6 +95,18 @@ def _declare(lib):
         "pbr_fma_probe": (C.c_int, [vp, i32, i32, C.POINTER(f64), vp]),
         "pbr_reduce_terms_static": (C.c_int, [vp, vp, vp, vp, i64, f64, vp, vp]),
         "pbr_reduce_terms_static_max_samples": (i64, []),
+        "pbr_flow_prepare": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp]),
+        "pbr_flow_apply": (C.c_int, [vp, vp, vp, i64, i32, i32, i32, vp, vp, vp]),
+        "pbr_flow_layer_forward": (C.c_int, [C.POINTER(PbrFlowLayer), i32, i64, vp, vp,
+                                             C.POINTER(PbrFlowSave), vp]),
+        "pbr_flow_layer_backward": (C.c_int, [C.POINTER(PbrFlowLayer), i64, vp, vp,
+                                              C.POINTER(PbrFlowSave), vp, vp, vp, vp]),
+        "pbr_gemm_tn_acc": (C.c_int, [vp, vp, i64, i32, i32, C.c_float, vp, vp, vp]),
+        "pbr_gemm_tn_scratch": (i64, [i64, i32, i32]),
+        "pbr_colsum": (C.c_int, [vp, i64, i32, vp, vp]),
+        "pbr_flow_base": (C.c_int, [vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "pbr_flow_weights": (C.c_int, [vp, vp, vp, vp, i64, vp, vp]),
+        "pbr_adam": (C.c_int, [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

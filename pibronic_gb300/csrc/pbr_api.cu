@@ -2,10 +2,11 @@
 #include <algorithm>
 #include <cstring>
 
-#include "pbr_fused.cuh"
+#include "pbr_team.cuh"
 
 namespace pbr {
 template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
+template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
 }
 
 namespace {
@@ -24,13 +25,56 @@ int ilog2(int x) {
     return l;
 }
 
+int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
+             uint64_t offset, const pbr_outputs* out, cudaStream_t st) {
+    using namespace pbr;
+    TeamArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.m = m;
+    a.q_in = q_in;
+    a.X = X;
+    a.out = *out;
+    a.key0 = static_cast<uint32_t>(seed);
+    a.key1 = static_cast<uint32_t>(seed >> 32);
+    a.offset = offset;
+    a.rs = row_stride(m.P);
+    a.qstride = m.N * a.rs + 1;
+    a.rl = record_len(m.A, m.K);
+    const int esz = m.precision == 32 ? 4 : 8;
+    const int TA = pow2_ceil(m.A);
+    const int max_teams = kTeamThreads / TA;
+    a.S = std::max(1, kTeamThreads / m.P);
+    while (true) {
+        // teams per sample: the largest power of two that the threads hold and the ring can use
+        a.G = 1;
+        while (a.G * 2 <= max_teams / a.S && a.G * 2 <= m.P) a.G *= 2;
+        const TeamPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.G, a.qstride, a.rl);
+        if (plan.total_bytes <= kMaxSmem) break;
+        if (a.S == 1) return PBR_ERR_UNSUPPORTED;
+        a.S = std::max(1, a.S / 2);
+    }
+    a.C = (m.P + a.G - 1) / a.G;
+    switch (m.A) {
+        case 1: return launch_team<1>(m.K, qmode, m.precision, a, st);
+        case 2: return launch_team<2>(m.K, qmode, m.precision, a, st);
+        case 3: return launch_team<3>(m.K, qmode, m.precision, a, st);
+        case 4: return launch_team<4>(m.K, qmode, m.precision, a, st);
+        case 5: return launch_team<5>(m.K, qmode, m.precision, a, st);
+        case 6: return launch_team<6>(m.K, qmode, m.precision, a, st);
+        case 7: return launch_team<7>(m.K, qmode, m.precision, a, st);
+        case 8: return launch_team<8>(m.K, qmode, m.precision, a, st);
+        default: return PBR_ERR_UNSUPPORTED;
+    }
+}
+
 int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, uint64_t seed,
               uint64_t offset, const pbr_outputs* out, void* stream) {
     using namespace pbr;
     if (!model || !out || X < 0) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const pbr_model& m = *model;
-    if (m.A < 1 || m.A > 4) return PBR_ERR_UNSUPPORTED;
+    if (m.A < 1 || m.A > PBR_MAX_A) return PBR_ERR_UNSUPPORTED;
+    if (m.variant < 0 || m.variant > 2) return PBR_ERR_ARG;
     if (m.A_rho < m.A || m.A_rho > PBR_MAX_A_RHO) return PBR_ERR_ARG;
     if (m.n_fill_rho != m.A) return PBR_ERR_ARG;
     if (m.N < 1 || m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P) return PBR_ERR_ARG;
@@ -41,8 +85,11 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     if (!m.vib_cs || !m.vib_th || !m.vib_c || !m.vib_d || !m.vib_e || !m.vib_l || !m.vib_qq ||
         !m.rho_cs || !m.rho_th || !m.rho_c || !m.rho_d)
         return PBR_ERR_ARG;
-    if (qmode == kSample && (!m.mode_std || !m.src_cdf)) return PBR_ERR_ARG;
+    if (qmode == kSample && (!m.ring_chol || !m.src_cdf)) return PBR_ERR_ARG;
     if (qmode != kSample && !q_in) return PBR_ERR_ARG;
+    const bool team = m.variant == 2 || (m.variant == 0 && m.A > 4);
+    if (team) return run_team(m, qmode, q_in, X, seed, offset, out, static_cast<cudaStream_t>(stream));
+    if (m.A > 4) return PBR_ERR_UNSUPPORTED;
 
     FusedArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -70,7 +117,7 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     }
     a.logG = ilog2(a.G);
     a.C = (m.P + a.G - 1) / a.G;
-    if (qmode == kSample && a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;   // P > 256
+
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     switch (m.A) {
         case 1: return launch_fused<1>(m.K, qmode, m.precision, a, st);
@@ -108,7 +155,7 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
     if (X == 0) return PBR_OK;
     const pbr_model& m = *model;
     if (m.N < 1 || m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P) return PBR_ERR_ARG;
-    if (m.A_rho < 1 || m.A_rho > PBR_MAX_A_RHO || !m.mode_std || !m.src_cdf || !m.rho_d) return PBR_ERR_ARG;
+    if (m.A_rho < 1 || m.A_rho > PBR_MAX_A_RHO || !m.ring_chol || !m.src_cdf || !m.rho_d) return PBR_ERR_ARG;
     if (m.precision != 32 && m.precision != 64) return PBR_ERR_ARG;
     FusedArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -126,14 +173,13 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
     int bytes = 0;
     while (true) {
         a.S = kThreads / a.G;
-        bytes = static_cast<int>((align_up(2 * m.P, 4) + a.S * a.qstride) * esz);
+        bytes = static_cast<int>(a.S * a.qstride * esz);
         if (bytes <= kMaxSmem || a.G == 32) break;
         a.G *= 2;
     }
     if (bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
     a.logG = ilog2(a.G);
     a.C = (m.P + a.G - 1) / a.G;
-    if (a.C > kMaxChunk) return PBR_ERR_UNSUPPORTED;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto go = [&](auto kern) -> int {
         if (bytes > 48 * 1024 &&

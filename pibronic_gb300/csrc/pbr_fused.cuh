@@ -25,7 +25,7 @@
 namespace pbr {
 
 constexpr int kThreads = 128;
-constexpr int kMaxChunk = 8;       // beads per thread on the sampling path
+constexpr int kMaxChunk = 8;       // target beads per thread (chunk length) of the ring product
 enum QMode : int { kSample = 0, kQ64 = 1, kQ32 = 2 };
 
 struct FusedArgs {
@@ -56,14 +56,13 @@ __host__ __device__ inline int rec_len(int A, int K) {
 
 // Shared-memory plan (in elements of the table type, esz bytes each); identical on host and device.
 struct SmemPlan {
-    int c, e, qq, rc, rec, trig, q, qlo, total_bytes;
+    int c, e, qq, rc, rec, q, qlo, total_bytes;
     __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int S, int qstride) {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
         c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
         rec = take(N * rec_len(A, K));
-        trig = take(qm == kSample ? 2 * P : 0);
         q = take(S * qstride);
         qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
         total_bytes = o * esz;
@@ -190,113 +189,67 @@ template <> struct LogSum<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
-// Phase A on the sampling path: the G threads of one sample (lanes gmask) draw the source surface
-// and the normal-mode coordinates and transform them to bead coordinates q[j][p] in shared
-// memory (layout qidx).  Returns the source surface.  pimc.py:326-334, 386-389, 613-631.
+// Source surface of global sample sg ~ Categorical(state weights) (pimc.py:386-389).
 template <typename T>
-__device__ int draw_sample_smem(const pbr_model& m, const T* s_trig, T* qs, int rs, int64_t sidx,
-                                uint64_t offset, uint32_t key0, uint32_t key1, int g, int G, int C,
-                                int p_begin, unsigned gmask) {
-    const int N = m.N, P = m.P;
-    const uint64_t sg = offset + static_cast<uint64_t>(sidx);
-    const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
-    // source surface ~ Categorical(state weights) (pimc.py:386-389)
-    const u32x4 rs4 = philox4x32_10(u32x4{0xFFFFFFFFu, lo, hi, 1u}, key0, key1);
-    const float us = u01(rs4.x);
+__device__ __forceinline__ int draw_source(const pbr_model& m, uint64_t sg, uint32_t key0, uint32_t key1) {
+    const u32x4 r = philox4x32_10(u32x4{0xFFFFFFFFu, static_cast<uint32_t>(sg),
+                                        static_cast<uint32_t>(sg >> 32), 1u}, key0, key1);
+    const float u = u01(r.x);
     const T* cdf = static_cast<const T*>(m.src_cdf);
     int src = 0;
-    for (int a = 0; a < m.A_rho - 1; ++a) src += (us >= static_cast<float>(cdf[a])) ? 1 : 0;
-    // normal-mode coordinates cc[j][s] ~ Normal(0, std[src][j][s]) (pimc.py:326-334)
-    const T* stdp = static_cast<const T*>(m.mode_std) + static_cast<int64_t>(src) * N * P;
-    const int NP = N * P;
-    const int ncalls = (NP + 3) >> 2;
-    for (int cidx = g; cidx < ncalls; cidx += G) {
-        const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(cidx), lo, hi, 0u}, key0, key1);
+    for (int a = 0; a < m.A_rho - 1; ++a) src += (u >= static_cast<float>(cdf[a])) ? 1 : 0;
+    return src;
+}
+
+// Bead coordinates of mode j of global sample sg (pimc.py:326-334, 613-631): standard normals
+// z_p (Philox counter (j * ceil(P/4) + p/4, sample), Box-Muller) and back substitution
+// x = L^-T z through the cyclic-tridiagonal factor of rho's bead precision,
+//   x_p = a_p (z_p - b_p x_{p+1} - c_p x_{P-1}),  q_p = x_p + d_src,j,
+// written to the sample's shared-memory row (layout qidx).  The distribution is rho's
+// N(d_src, Lambda^-1), the one the reference draws in normal modes.
+template <typename T>
+__device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t key0, uint32_t key1,
+                                T dsh, T* qs, int rs) {
+    const int N = m.N, P = m.P;
+    const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
+    const T* b = a + static_cast<int64_t>(N) * P;
+    const T* c = b + static_cast<int64_t>(N) * P;
+    const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
+    const int CP = (P + 3) >> 2;
+    T xnext = T(0), xlast = T(0);
+    for (int p4 = (P - 1) >> 2; p4 >= 0; --p4) {
+        const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(j * CP + p4), lo, hi, 0u}, key0, key1);
         float z[4];
         box_muller(r.x, r.y, z[0], z[1]);
         box_muller(r.z, r.w, z[2], z[3]);
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int i = 4 * cidx + t;
-            if (i < NP) {
-                const int j = i / P, sl = i - j * P;
-                qs[qidx(j, sl, rs)] = T(z[t]) * stdp[i];
+        for (int t = 3; t >= 0; --t) {
+            const int p = 4 * p4 + t;
+            if (p >= P) continue;
+            T x;
+            if (p == P - 1) {
+                x = __ldg(a + p) * T(z[t]);
+                xlast = x;
+            } else {
+                x = __ldg(a + p) * (T(z[t]) - __ldg(b + p) * xnext - __ldg(c + p) * xlast);
             }
+            xnext = x;
+            qs[qidx(j, p, rs)] = x + dsh;
         }
     }
-    __syncwarp(gmask);
-    // ring transform q_p = sum_s B_ps cc_s + d^rho_src (pimc.py:618-624), in place per mode block
-    const T inv_sqrt_p = T(1.0 / sqrt(static_cast<double>(P)));
-    const int kmax = (P - 1) / 2;
-    const bool even = (P % 2) == 0;
-    const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * N;
-    constexpr int JB = 4;
-    for (int j0 = 0; j0 < N; j0 += JB) {
-        T acc[kMaxChunk][JB];
-#pragma unroll
-        for (int b = 0; b < kMaxChunk; ++b) {
-            const int p = p_begin + b;
-#pragma unroll
-            for (int jj = 0; jj < JB; ++jj) {
-                const int j = min(j0 + jj, N - 1);
-                T v = qs[qidx(j, 0, rs)] * inv_sqrt_p;
-                if (even) {
-                    const T ny = qs[qidx(j, P - 1, rs)] * inv_sqrt_p;
-                    v += (p & 1) ? -ny : ny;
-                }
-                acc[b][jj] = v;
-            }
-        }
-        int mm[kMaxChunk];
-#pragma unroll
-        for (int b = 0; b < kMaxChunk; ++b) mm[b] = 0;
-        for (int k = 1; k <= kmax; ++k) {
-            T cc_c[JB], cc_s[JB];
-#pragma unroll
-            for (int jj = 0; jj < JB; ++jj) {
-                const int j = min(j0 + jj, N - 1);
-                cc_c[jj] = qs[qidx(j, 2 * k - 1, rs)];
-                cc_s[jj] = qs[qidx(j, 2 * k, rs)];
-            }
-#pragma unroll
-            for (int b = 0; b < kMaxChunk; ++b) {
-                const int p = p_begin + b;
-                int mb = mm[b] + p;                    // (k p) mod P, incremental
-                mb = (mb >= P) ? mb - P : mb;
-                mb = (mb >= P) ? mb % P : mb;
-                mm[b] = mb;
-                const T cth = s_trig[2 * mb], sth = s_trig[2 * mb + 1];
-#pragma unroll
-                for (int jj = 0; jj < JB; ++jj) acc[b][jj] = fma(cc_c[jj], cth, fma(cc_s[jj], sth, acc[b][jj]));
-            }
-        }
-        __syncwarp(gmask);
-#pragma unroll
-        for (int b = 0; b < kMaxChunk; ++b) {
-            const int p = p_begin + b;
-            if (b < C && p < P) {
-#pragma unroll
-                for (int jj = 0; jj < JB; ++jj) {
-                    const int j = j0 + jj;
-                    if (j < N) qs[qidx(j, p, rs)] = acc[b][jj] + dsrc[j];
-                }
-            }
-        }
-        __syncwarp(gmask);
-    }
-    return src;
 }
 
-// Fill the sampling-path trig table: trig[2m], trig[2m+1] = sqrt(2/P) (cos, sin)(2 pi m / P).
+// Phase A on the sampling path of the chunk form: the G threads of one sample (lanes gmask)
+// each draw the modes j = g, g + G, ...; returns the source surface.
 template <typename T>
-__device__ void fill_trig(T* s_trig, int P) {
-    const double amp = sqrt(2.0 / P);
-    for (int i = threadIdx.x; i < P; i += blockDim.x) {
-        double s, c;
-        sincospi(2.0 * i / P, &s, &c);
-        s_trig[2 * i] = T(amp * c);
-        s_trig[2 * i + 1] = T(amp * s);
-    }
+__device__ int draw_sample_smem(const pbr_model& m, T* qs, int rs, int64_t sidx, uint64_t offset,
+                                uint32_t key0, uint32_t key1, int g, int G, unsigned gmask) {
+    const uint64_t sg = offset + static_cast<uint64_t>(sidx);
+    const int src = draw_source<T>(m, sg, key0, key1);
+    const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * m.N;
+    for (int j = g; j < m.N; j += G) draw_mode_chain<T>(m, j, sg, key0, key1, dsrc[j], qs, rs);
+    __syncwarp(gmask);
+    return src;
 }
 
 // power-of-two renormalisation of a series matrix; returns the exponent taken out
@@ -336,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
     const int G = args.G, C = args.C, S = args.S;
     const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, args.qstride);
     T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
-    T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec; T* s_trig = sm + plan.trig;
+    T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec;
 
     // ---- model tables -> shared memory (once per CTA; the grid is persistent) -----------------
     {
@@ -366,7 +319,6 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
             else if (o >= 2 * KP + 2 * AP + 4) { const int pr = o - 2 * KP - 2 * AP - 4; if (pr < A2) v = g_l[j * A2 + pr]; }
             s_rec[i] = v;
         }
-        if (QM == kSample) fill_trig<T>(s_trig, P);
     }
     __syncthreads();
 
@@ -390,8 +342,8 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
         if (active) {
             const int NP = N * P;
             if (QM == kSample) {
-                const int src = draw_sample_smem<T>(m, s_trig, qs, rs, sidx, args.offset, args.key0,
-                                                    args.key1, g, G, C, p_begin, gmask);
+                const int src = draw_sample_smem<T>(m, qs, rs, sidx, args.offset, args.key0,
+                                                    args.key1, g, G, gmask);
                 if (args.out.src_out && g == 0) args.out.src_out[sidx] = src;
                 if (args.out.q_out) {
                     float* qo = args.out.q_out + sidx * static_cast<int64_t>(NP);
@@ -709,20 +661,17 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 template <typename T>
 __global__ void __launch_bounds__(kThreads) sample_q_kernel(const FusedArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* s_trig = reinterpret_cast<T*>(smem_raw);
     const pbr_model& m = args.m;
-    const int N = m.N, P = m.P, G = args.G, C = args.C, S = args.S, rs = args.rs;
-    fill_trig<T>(s_trig, P);
-    __syncthreads();
+    const int N = m.N, P = m.P, G = args.G, S = args.S, rs = args.rs;
     const int tid = threadIdx.x, grp = tid >> args.logG, g = tid & (G - 1), lane = tid & 31;
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-    T* qs = s_trig + align_up(2 * P, 4) + grp * args.qstride;
+    T* qs = reinterpret_cast<T*>(smem_raw) + grp * args.qstride;
     for (int64_t base = static_cast<int64_t>(blockIdx.x) * S; base < args.X;
          base += static_cast<int64_t>(gridDim.x) * S) {
         const int64_t sidx = base + grp;
         if (sidx < args.X) {
-            const int src = draw_sample_smem<T>(m, s_trig, qs, rs, sidx, args.offset, args.key0,
-                                                args.key1, g, G, C, g * C, gmask);
+            const int src = draw_sample_smem<T>(m, qs, rs, sidx, args.offset, args.key0, args.key1,
+                                                g, G, gmask);
             if (args.out.src_out && g == 0) args.out.src_out[sidx] = src;
             const int NP = N * P;
             float* qo = args.out.q_out + sidx * static_cast<int64_t>(NP);

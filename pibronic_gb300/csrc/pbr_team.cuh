@@ -1,0 +1,523 @@
+// pbr_team.cuh -- the fused PIMC block evaluation, bead-parallel / row-team form.
+//
+// One CTA of kTeamThreads threads evaluates S samples per tile in four block-synchronised phases:
+//
+//   A   q[j][p] of the tile's samples into shared memory (device sampler, block-cooperative:
+//       sources, Philox normals, real-Fourier ring transform; or the caller's q).
+//   B1  one thread per (sample, bead): O-matrix exponents of rho and the coupled model (beta
+//       series of order K), ln S12, the scaled O series, V(q_p), Jacobi, M_p = U exp(-tau lambda) U^T;
+//       written to a per-bead record in shared memory.
+//   B2  a team of TA = pow2ceil(A) threads per bead chunk, thread r owning row r of the series
+//       matrices N_k: N(h) <- N(h) M_p diag(O_p(h)) over the chunk, power-of-two renormalised.
+//   C   chunk products combined in bead order through shared memory (log2 G levels).
+//   D   traces, rho, g(beta +- db) in FP64; one team per sample writes the outputs.
+//
+// Registers per thread stay near the B1 working set (V, Jacobi, one bead's series), so far more
+// warps are resident than in the register-resident chunk form, and A up to 8 fits.
+#pragma once
+
+#include "pbr_fused.cuh"
+
+namespace pbr {
+
+constexpr int kTeamThreads = 256;
+
+struct TeamArgs {
+    pbr_model m;
+    const void* q_in;
+    int64_t X;
+    pbr_outputs out;
+    uint32_t key0, key1;
+    uint64_t offset;
+    int S;          // samples per tile
+    int G;          // teams (bead chunks) per sample, a power of two
+    int C;          // beads per team
+    int rs;         // q row stride (skewed layout, qidx)
+    int qstride;    // q elements per sample
+    int rl;         // bead record length
+};
+
+__host__ __device__ inline int pow2_ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// bead record: [M: A*A][O series: (K+1)*A][ln S12][M exponent][rho log terms: A] padded to 4
+__host__ __device__ inline int record_len(int A, int K) { return align_up(A * A + (K + 1) * A + 2 + A, 4); }
+
+struct TeamPlan {
+    int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
+    __host__ __device__ TeamPlan(int A, int K, int qm, int esz, int N, int P, int S, int G, int qstride,
+                                 int rl) {
+        const int A2P = align_up(npair(A), 4);
+        int o = 0;
+        auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
+        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
+        rec = take(N * rec_len(A, K));
+        src = take(S);                                             // ints stored in the slot
+        q = take(S * qstride);
+        qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
+        const int comb = S * G * ((K + 1) * A * A + 4);
+        int nb = S * P * rl;
+        nb = nb > comb ? nb : comb;
+        beads = take(nb);
+        lsums = take((S * G * (A + 2) * 8 + esz - 1) / esz);      // doubles + exponent slot
+        total_bytes = o * esz;
+    }
+};
+
+template <int A, int K, int QM, typename T>
+__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kernel(const TeamArgs args) {
+    constexpr int A2 = npair(A);
+    constexpr int A2P = (A2 + 3) / 4 * 4;
+    constexpr int KP = (K + 1 + 3) / 4 * 4;
+    constexpr int AP = (A + 3) / 4 * 4;
+    constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
+    constexpr int TA = (A <= 1) ? 1 : (A <= 2) ? 2 : (A <= 4) ? 4 : 8;
+    constexpr int OFF_O = A * A, OFF_L = A * A + (K + 1) * A, OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
+    constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
+    constexpr int NT = kTeamThreads;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+
+    const pbr_model& m = args.m;
+    const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
+    const int S = args.S, G = args.G, C = args.C, RL = args.rl;
+    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, G, args.qstride, RL);
+    T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
+    T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec;
+    int* s_src = reinterpret_cast<int*>(sm + plan.src);
+    T* s_q = sm + plan.q;
+    T* s_ql = kLo ? sm + plan.qlo : nullptr;
+    T* s_beads = sm + plan.beads;
+    double* s_lsum = reinterpret_cast<double*>(sm + plan.lsums);
+    const int tid = threadIdx.x;
+
+    // ---- model tables -> shared memory (once per CTA; the grid is persistent) -----------------
+    {
+        const T* g_cs = static_cast<const T*>(m.vib_cs);  const T* g_th = static_cast<const T*>(m.vib_th);
+        const T* g_c = static_cast<const T*>(m.vib_c);    const T* g_d = static_cast<const T*>(m.vib_d);
+        const T* g_e = static_cast<const T*>(m.vib_e);    const T* g_l = static_cast<const T*>(m.vib_l);
+        const T* g_qq = static_cast<const T*>(m.vib_qq);
+        const T* g_rcs = static_cast<const T*>(m.rho_cs); const T* g_rth = static_cast<const T*>(m.rho_th);
+        const T* g_rc = static_cast<const T*>(m.rho_c);   const T* g_rd = static_cast<const T*>(m.rho_d);
+        for (int i = tid; i < (K + 1) * A; i += NT) s_c[i] = g_c[i];
+        for (int i = tid; i < A2P; i += NT) s_e[i] = (i < A2) ? g_e[i] : T(0);
+        const int N2 = npair(N);
+        for (int i = tid; i < N2 * A2P; i += NT) {
+            const int row = i / A2P, col = i - row * A2P;
+            s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
+        }
+        for (int i = tid; i < A; i += NT) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
+        for (int i = tid; i < N * MR; i += NT) {
+            const int j = i / MR, o = i - j * MR;
+            T v = T(0);
+            if (o < KP) { if (o <= K) v = g_cs[o * N + j]; }
+            else if (o < 2 * KP) { if (o - KP <= K) v = g_th[(o - KP) * N + j]; }
+            else if (o < 2 * KP + AP) { const int a = o - 2 * KP; if (a < A) v = g_d[a * N + j]; }
+            else if (o < 2 * KP + 2 * AP) { const int a = o - 2 * KP - AP; if (a < nfill) v = g_rd[a * N + j]; }
+            else if (o == 2 * KP + 2 * AP) v = g_rcs[j];
+            else if (o == 2 * KP + 2 * AP + 1) v = g_rth[j];
+            else if (o >= 2 * KP + 2 * AP + 4) { const int pr = o - 2 * KP - 2 * AP - 4; if (pr < A2) v = g_l[j * A2 + pr]; }
+            s_rec[i] = v;
+        }
+    }
+    __syncthreads();
+
+    const T tau_l2 = T(m.tau * 1.4426950408889634);   // tau * log2(e)
+    const int NP = N * P;
+    // B2 / C / D thread roles
+    const int team = tid / TA, r = tid % TA;
+    const int ts = team / G, tc = team % G;               // sample slot and chunk of this team
+    const bool team_ok = team < S * G;
+    const int lane = tid & 31;
+    const unsigned tmask = (TA == 32) ? 0xffffffffu : (((1u << TA) - 1u) << (lane & ~(TA - 1)));
+    const int CL = (K + 1) * A * A + 4;                    // combine slot length
+
+    for (int64_t base = static_cast<int64_t>(blockIdx.x) * S; base < args.X;
+         base += static_cast<int64_t>(gridDim.x) * S) {
+        const int nvalid = static_cast<int>(min(static_cast<int64_t>(S), args.X - base));
+
+        // ================================ phase A ==============================================
+        if (QM == kSample) {
+            for (int s = tid; s < S; s += NT)
+                s_src[s] = (s < nvalid) ? draw_source<T>(m, args.offset + static_cast<uint64_t>(base + s),
+                                                         args.key0, args.key1) : 0;
+            __syncthreads();
+            // one back-substitution chain per (sample, mode)
+            for (int it = tid; it < nvalid * N; it += NT) {
+                const int s = it / N, j = it - s * N;
+                const T dsh = static_cast<const T*>(m.rho_d)[static_cast<int64_t>(s_src[s]) * N + j];
+                draw_mode_chain<T>(m, j, args.offset + static_cast<uint64_t>(base + s), args.key0,
+                                   args.key1, dsh, s_q + s * args.qstride, rs);
+            }
+            __syncthreads();
+            if (args.out.q_out || args.out.src_out) {
+                for (int i = tid; i < nvalid * NP; i += NT) {
+                    const int s = i / NP, ii = i - s * NP, j = ii / P, p = ii - j * P;
+                    if (args.out.q_out)
+                        args.out.q_out[(base + s) * static_cast<int64_t>(NP) + ii] =
+                            static_cast<float>(s_q[s * args.qstride + qidx(j, p, rs)]);
+                }
+                if (args.out.src_out)
+                    for (int s = tid; s < nvalid; s += NT) args.out.src_out[base + s] = s_src[s];
+            }
+        } else {
+            for (int i = tid; i < nvalid * NP; i += NT) {
+                const int s = i / NP, ii = i - s * NP, j = ii / P, p = ii - j * P;
+                const int dst = s * args.qstride + qidx(j, p, rs);
+                if (QM == kQ64) {
+                    const double v = static_cast<const double*>(args.q_in)[(base + s) * static_cast<int64_t>(NP) + ii];
+                    const T hi = T(v);
+                    s_q[dst] = hi;
+                    if (kLo) s_ql[dst] = T(v - static_cast<double>(hi));
+                } else {
+                    s_q[dst] = T(static_cast<const float*>(args.q_in)[(base + s) * static_cast<int64_t>(NP) + ii]);
+                }
+            }
+            __syncthreads();
+        }
+
+        // ================================ phase B1: bead records ===============================
+        for (int it = tid; it < nvalid * P; it += NT) {
+            const int s = it / P, p = it - s * P;
+            const int pn = (p + 1 == P) ? 0 : p + 1;
+            const T* qs = s_q + s * args.qstride;
+            const T* ql = kLo ? s_ql + s * args.qstride : nullptr;
+            const int ip = qidx(0, p, rs), ipn = qidx(0, pn, rs);
+            T* rec_out = s_beads + static_cast<int64_t>(it) * RL;
+            T phv[K + 1][A], phr[A], v[A2P];
+#pragma unroll
+            for (int k = 0; k <= K; ++k)
+#pragma unroll
+                for (int a = 0; a < A; ++a) phv[k][a] = s_c[k * A + a];
+#pragma unroll
+            for (int a = 0; a < A; ++a) phr[a] = s_rc[a];
+            ldv(s_e, v);
+            T dsum[K + 1];
+#pragma unroll
+            for (int k = 0; k <= K; ++k) dsum[k] = T(0);
+            T rdsum = T(0);
+            for (int j = 0; j < N; ++j) {
+                const T* rec = s_rec + j * MR;
+                T cs[KP], th[KP], dv[AP], rdv[AP], rx[4], lr[A2P];
+                ldv(rec, cs);
+                ldv(rec + KP, th);
+                ldv(rec + 2 * KP, dv);
+                ldv(rec + 2 * KP + AP, rdv);
+                ldv(rec + 2 * KP + 2 * AP, rx);
+                ldv(rec + 2 * KP + 2 * AP + 4, lr);
+                const T qa = qs[ip + j * rs], qb = qs[ipn + j * rs];
+                T dq = qa - qb;
+                if (kLo) dq += ql[ip + j * rs] - ql[ipn + j * rs];
+                const T dq2 = dq * dq;
+#pragma unroll
+                for (int k = 0; k <= K; ++k) dsum[k] = fma(cs[k], dq2, dsum[k]);
+                rdsum = fma(rx[0], dq2, rdsum);
+#pragma unroll
+                for (int a = 0; a < A; ++a) {
+                    const T ua = qa - dv[a], ub = qb - dv[a];
+                    const T sq = fma(ua, ua, ub * ub);
+#pragma unroll
+                    for (int k = 0; k <= K; ++k) phv[k][a] = fma(-th[k], sq, phv[k][a]);
+                    if (a < nfill) {
+                        const T ra = qa - rdv[a], rb = qb - rdv[a];
+                        phr[a] = fma(-rx[1], fma(ra, ra, rb * rb), phr[a]);
+                    }
+                }
+#pragma unroll
+                for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
+            }
+            T lmax;
+            {
+#pragma unroll
+                for (int a = 0; a < A; ++a) {
+#pragma unroll
+                    for (int k = 0; k <= K; ++k) phv[k][a] -= dsum[k];
+                    phr[a] -= rdsum;
+                }
+                lmax = phv[0][0];
+#pragma unroll
+                for (int a = 1; a < A; ++a) lmax = max(lmax, phv[0][a]);
+#pragma unroll
+                for (int a = 0; a < A; ++a)
+                    if (a < nfill) lmax = max(lmax, phr[a]);
+                rec_out[OFF_L] = lmax;
+#pragma unroll
+                for (int a = 0; a < A; ++a) rec_out[OFF_R + a] = (a < nfill) ? phr[a] - lmax : T(0);
+#pragma unroll
+                for (int a = 0; a < A; ++a) {
+                    T ek[K + 1];
+                    ek[0] = T(1);
+#pragma unroll
+                    for (int k = 1; k <= K; ++k) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int i = 1; i <= k; ++i) acc = fma(T(i) * phv[i][a], ek[k - i], acc);
+                        ek[k] = acc * (T(1) / T(k));
+                    }
+                    const T e0 = dev_exp<T>(phv[0][a] - lmax);
+#pragma unroll
+                    for (int k = 0; k <= K; ++k) rec_out[OFF_O + k * A + a] = e0 * ek[k];
+                }
+            }
+            {
+                int row = 0;
+                for (int d = 0; d < N; ++d) {
+                    const T qd = qs[ip + d * rs];
+                    for (int e = 0; e <= d; ++e, ++row) {
+                        const T w = qd * qs[ip + e * rs];
+                        T qrow[A2P];
+                        ldv(s_qq + row * A2P, qrow);
+#pragma unroll
+                        for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                    }
+                }
+            }
+            {
+                T am[A][A], u[A][A];
+#pragma unroll
+                for (int b = 0; b < A; ++b)
+#pragma unroll
+                    for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
+#pragma unroll
+                for (int b = 0; b < A; ++b)
+#pragma unroll
+                    for (int c = 0; c < A; ++c) u[b][c] = (b == c) ? T(1) : T(0);
+                jacobi_accumulate<T, A>(am, u, sizeof(T) == 4 ? 12 : 16);
+                T t[A];
+                T tmax = -tau_l2 * am[0][0];
+#pragma unroll
+                for (int i = 0; i < A; ++i) { t[i] = -tau_l2 * am[i][i]; tmax = max(tmax, t[i]); }
+                const int n2 = static_cast<int>(floor(tmax));
+                rec_out[OFF_N] = T(n2);
+                T ev[A];
+#pragma unroll
+                for (int i = 0; i < A; ++i) ev[i] = dev_exp2<T>(t[i] - T(n2));
+#pragma unroll
+                for (int b = 0; b < A; ++b)
+#pragma unroll
+                    for (int c = 0; c <= b; ++c) {
+                        T acc = T(0);
+#pragma unroll
+                        for (int i = 0; i < A; ++i) acc = fma(u[b][i] * ev[i], u[c][i], acc);
+                        rec_out[b * A + c] = acc;
+                        rec_out[c * A + b] = acc;
+                    }
+            }
+        }
+        __syncthreads();
+
+        // ================================ phase B2: row teams over bead chunks =================
+        T nrow[K + 1][A];
+        int nexp = 0;
+        LogSum<T> lr, ls;
+        const bool tact = team_ok && ts < nvalid;
+        const int pb = tc * C, pe = min(P, pb + C);
+        if (tact) {
+#pragma unroll
+            for (int k = 0; k <= K; ++k)
+#pragma unroll
+                for (int c = 0; c < A; ++c) nrow[k][c] = (k == 0 && c == r) ? T(1) : T(0);
+            const T* recs = s_beads + static_cast<int64_t>(ts) * P * RL;
+            for (int p = pb; p < pe; ++p) {
+                const T* rc_ = recs + p * RL;
+                nexp += static_cast<int>(rc_[OFF_N]);
+                if (r == 0) ls.add(rc_[OFF_L]);
+                if (r < A && r < nfill) lr.add(rc_[OFF_R + (r < A ? r : 0)]);
+                if (r < A) {
+                    T mf[A * A], of[(K + 1) * A];
+                    ldv(rc_, mf);
+                    ldv(rc_ + OFF_O, of);
+                    T Mm[A][A], os[K + 1][A];
+#pragma unroll
+                    for (int b = 0; b < A; ++b)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) Mm[b][c] = mf[b * A + c];
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) os[k][c] = of[k * A + c];
+                    if (p == pb) {
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) {
+                                T mrc = T(0);
+#pragma unroll
+                                for (int b = 0; b < A; ++b) mrc = (b == r) ? Mm[b][c] : mrc;
+                                nrow[k][c] = mrc * os[k][c];
+                            }
+                    } else {
+                        T y[K + 1][A];
+#pragma unroll
+                        for (int i = 0; i <= K; ++i)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int mm = 0; mm < A; ++mm) acc = fma(nrow[i][mm], Mm[mm][c], acc);
+                                y[i][c] = acc;
+                            }
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int i = 0; i <= k; ++i) acc = fma(y[i][c], os[k - i][c], acc);
+                                nrow[k][c] = acc;
+                            }
+                    }
+                }
+                if (((p - pb) & 1) == 1 || p + 1 == pe) {
+                    // team-wide power-of-two renormalisation
+                    T mx = T(0);
+                    if (r < A) {
+#pragma unroll
+                        for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nrow[0][c]));
+                    }
+#pragma unroll
+                    for (int o = TA / 2; o >= 1; o >>= 1) mx = max(mx, __shfl_xor_sync(tmask, mx, o, TA));
+                    if (mx > T(0) && isfinite(mx)) {
+                        int e2;
+                        frexp(mx, &e2);
+                        const T sc = ldexp(T(1), -e2);
+                        nexp += e2;
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) nrow[k][c] *= sc;
+                    }
+                }
+            }
+            if (pb >= pe) {
+                // empty chunk: identity
+#pragma unroll
+                for (int k = 0; k <= K; ++k)
+#pragma unroll
+                    for (int c = 0; c < A; ++c) nrow[k][c] = (k == 0 && c == r) ? T(1) : T(0);
+            }
+        }
+        __syncthreads();     // every thread is done reading bead records: the combine slots reuse them
+
+        // ================================ phase C: combine chunks ==============================
+        T* comb = s_beads;
+        int* cexp = reinterpret_cast<int*>(s_lsum + S * G * (A + 1));
+        const int slot = ts * G + tc;
+        double lr_d = 0.0, ls_d = 0.0;
+        if (tact) {
+            lr_d = lr.value();
+            ls_d = ls.value();
+            if (r < A)
+#pragma unroll
+                for (int k = 0; k <= K; ++k)
+#pragma unroll
+                    for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
+            if (r < A) s_lsum[slot * (A + 1) + r] = lr_d;
+            if (r == 0) { s_lsum[slot * (A + 1) + A] = ls_d; cexp[slot] = nexp; }
+        }
+        __syncthreads();
+        for (int st = 1; st < G; st <<= 1) {
+            const bool recv = tact && (tc % (2 * st)) == 0 && tc + st < G;
+            if (recv) {
+                const int ps = slot + st;
+                const T* Y = comb + ps * CL;
+                if (r < A) {
+                    T z[K + 1][A];
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) {
+                            T acc = T(0);
+#pragma unroll
+                            for (int i = 0; i <= k; ++i)
+#pragma unroll
+                                for (int mm = 0; mm < A; ++mm) acc = fma(nrow[i][mm], Y[((k - i) * A + mm) * A + c], acc);
+                            z[k][c] = acc;
+                        }
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) nrow[k][c] = z[k][c];
+                    lr_d += s_lsum[ps * (A + 1) + r];
+                }
+                if (r == 0) ls_d += s_lsum[ps * (A + 1) + A];
+                nexp += cexp[ps];
+                T mx = T(0);
+                if (r < A) {
+#pragma unroll
+                    for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nrow[0][c]));
+                }
+#pragma unroll
+                for (int o = TA / 2; o >= 1; o >>= 1) mx = max(mx, __shfl_xor_sync(tmask, mx, o, TA));
+                if (mx > T(0) && isfinite(mx)) {
+                    int e2;
+                    frexp(mx, &e2);
+                    const T sc = ldexp(T(1), -e2);
+                    nexp += e2;
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) nrow[k][c] *= sc;
+                }
+                // own slot is no other receiver's partner at this level: write it back now
+                if (r < A)
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
+                if (r < A) s_lsum[slot * (A + 1) + r] = lr_d;
+                if (r == 0) { s_lsum[slot * (A + 1) + A] = ls_d; cexp[slot] = nexp; }
+            }
+            __syncthreads();
+        }
+
+        // ================================ phase D: outputs =====================================
+        if (tact && tc == 0) {
+            double coef[K + 1];
+#pragma unroll
+            for (int k = 0; k <= K; ++k) {
+                double d = 0.0;
+#pragma unroll
+                for (int c = 0; c < A; ++c) d = (c == r) ? static_cast<double>(nrow[k][c]) : d;
+                if (r >= A) d = 0.0;
+#pragma unroll
+                for (int o = TA / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, TA);
+                coef[k] = ldexp(d, nexp);
+            }
+            double rho = (r < A && r < nfill) ? exp(lr_d) : 0.0;
+#pragma unroll
+            for (int o = TA / 2; o >= 1; o >>= 1) rho += __shfl_xor_sync(tmask, rho, o, TA);
+            if (r == 0) {
+                const int64_t sidx = base + ts;
+                const pbr_outputs& o = args.out;
+                o.s_rho[sidx] = rho;
+                o.s_g[sidx] = coef[0];
+                bool bad = !isfinite(rho) || !isfinite(coef[0]);
+                if (K > 0) {
+                    const double db = m.delta_beta;
+                    double gp = 0.0, gm = 0.0;
+#pragma unroll
+                    for (int k = K; k >= 0; --k) { gp = gp * db + coef[k]; gm = gm * (-db) + coef[k]; }
+                    if (o.s_gp) o.s_gp[sidx] = gp;
+                    if (o.s_gm) o.s_gm[sidx] = gm;
+                    bad = bad || !isfinite(gp) || !isfinite(gm);
+                }
+                if (o.g_coef) {
+#pragma unroll
+                    for (int k = 0; k <= K; ++k) o.g_coef[sidx * (K + 1) + k] = coef[k];
+                }
+                if (o.log_scale) o.log_scale[sidx] = ls_d + static_cast<double>(P) * m.log_c0;
+                if (bad) flag_status(o.status, PBR_ERR_NONFINITE);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int A>
+int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStream_t stream);
+
+}  // namespace pbr

@@ -1,0 +1,56 @@
+// pbr_team_launch.cuh -- host launcher for the row-team kernel, included once per surface count.
+#pragma once
+
+#include <algorithm>
+
+#include "pbr_team.cuh"
+
+namespace pbr {
+
+template <int A, int K, int QM, typename T>
+static int launch_team_one(const TeamArgs& args, cudaStream_t stream) {
+    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
+                        args.qstride, args.rl);
+    auto kern = pimc_team_kernel<A, K, QM, T>;
+    static int configured = 0;
+    if (plan.total_bytes > 48 * 1024 && plan.total_bytes > configured) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 plan.total_bytes) != cudaSuccess)
+            return PBR_ERR_UNSUPPORTED;
+        configured = plan.total_bytes;
+    }
+    int dev = 0, sms = 0, occ = 0;
+    PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
+    PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTeamThreads,
+                                                                     plan.total_bytes));
+    if (occ < 1) return PBR_ERR_UNSUPPORTED;
+    const int64_t need = (args.X + args.S - 1) / args.S;
+    const int grid = static_cast<int>(std::min<int64_t>(need, static_cast<int64_t>(occ) * sms));
+    if (grid <= 0) return PBR_OK;
+    kern<<<grid, kTeamThreads, plan.total_bytes, stream>>>(args);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+template <int A>
+int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStream_t stream) {
+    if (precision == 32) {
+        if (K == 0) {
+            if (qmode == kSample) return launch_team_one<A, 0, kSample, float>(args, stream);
+            if (qmode == kQ64) return launch_team_one<A, 0, kQ64, float>(args, stream);
+            return launch_team_one<A, 0, kQ32, float>(args, stream);
+        }
+        if (qmode == kSample) return launch_team_one<A, 4, kSample, float>(args, stream);
+        if (qmode == kQ64) return launch_team_one<A, 4, kQ64, float>(args, stream);
+        return launch_team_one<A, 4, kQ32, float>(args, stream);
+    }
+    if (qmode == kQ32) return PBR_ERR_UNSUPPORTED;
+    if (K == 0) {
+        if (qmode == kSample) return launch_team_one<A, 0, kSample, double>(args, stream);
+        return launch_team_one<A, 0, kQ64, double>(args, stream);
+    }
+    if (qmode == kSample) return launch_team_one<A, 4, kSample, double>(args, stream);
+    return launch_team_one<A, 4, kQ64, double>(args, stream);
+}
+
+}  // namespace pbr

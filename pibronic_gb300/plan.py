@@ -121,6 +121,28 @@ def ring_mode_basis(P):
     return B
 
 
+def ring_precision_factor(omega, tau, P):
+    """Back-substitution coefficients of the bead-space precision of rho for each mode,
+    Lambda_j = 2 coth(tau w_j) I - csch(tau w_j) C (pimc.py:402-404 in the normal-mode basis).
+    Lambda_j is cyclic tridiagonal, so its Cholesky factor L is bidiagonal plus a dense last row,
+    and x = L^-T z solves as x_p = a_p (z_p - b_p x_{p+1} - c_p x_{P-1}).  Returns (3, N, P):
+    a = 1/L_pp, b_p = L_{p+1,p} (p <= P-3) and L_{P-1,P-2} (p = P-2), c_p = L_{P-1,p} (p <= P-3)."""
+    omega = np.asarray(omega, dtype=F64)
+    N = omega.shape[0]
+    C = np.zeros((P, P))
+    for p in range(P):
+        C[p, (p + 1) % P] = C[p, (p - 1) % P] = 1.0
+    out = np.zeros((3, N, P))
+    for j in range(N):
+        lam = 2.0 / np.tanh(tau * omega[j]) * np.eye(P) - C / np.sinh(tau * omega[j])
+        L = np.linalg.cholesky(lam)
+        out[0, j] = 1.0 / np.diag(L)
+        out[1, j, :P - 2] = np.array([L[p + 1, p] for p in range(P - 2)])
+        out[1, j, P - 2] = L[P - 1, P - 2]
+        out[2, j, :P - 2] = L[P - 1, :P - 2]
+    return out
+
+
 def pair_index(b, c):
     return b * (b + 1) // 2 + c
 
@@ -197,16 +219,12 @@ class PreparedModels:
                             qq[row, pair_index(b, c)] = 0.5 * Q[d, d, b, c]
                         else:
                             qq[row, pair_index(b, c)] = 0.5 * (Q[d, e_, b, c] + Q[e_, d, b, c])
-        lam = ring_mode_eigenvalues(P)
-        coth_r = 1.0 / np.tanh(self.tau * self.rho_omega)
-        csch_r = 1.0 / np.sinh(self.tau * self.rho_omega)
-        invcov = 2.0 * coth_r[None, :, None] - csch_r[None, :, None] * lam[None, None, :]  # pimc.py:402
-        mode_std = np.broadcast_to(np.sqrt(1.0 / invcov), (Ar, N, P)).copy()
+        ring_chol = ring_precision_factor(self.rho_omega, self.tau, P)
         return {
             "vib_cs": 0.5 * csch_s.T.copy(), "vib_th": 0.5 * tanh_s.T.copy(), "vib_c": vib_c.T.copy(),
             "vib_d": self.vib_shift.copy(), "vib_e": e, "vib_l": lt.reshape(N, A2), "vib_qq": qq,
             "rho_cs": 0.5 * rcsch[:, 0], "rho_th": 0.5 * rtanh[:, 0], "rho_c": rho_c,
-            "rho_d": self.rho_shift.copy(), "mode_std": mode_std,
+            "rho_d": self.rho_shift.copy(), "ring_chol": ring_chol,
             "src_cdf": np.cumsum(self.state_weight), "log_c0": log_c0,
         }
 
@@ -215,12 +233,17 @@ class DevicePlan:
     """The device-resident tables of one PreparedModels and the pbr_model struct pointing at them."""
 
     FIELDS = ("vib_cs", "vib_th", "vib_c", "vib_d", "vib_e", "vib_l", "vib_qq", "rho_cs", "rho_th",
-              "rho_c", "rho_d", "mode_std", "src_cdf")
+              "rho_c", "rho_d", "ring_chol", "src_cdf")
 
-    def __init__(self, prep, precision=32, device=None):
+    #: fused-kernel forms (pbr_model.variant): register-resident chunks (A <= 4) or bead-parallel
+    #: records + row teams (A <= 8); 0 lets the library choose
+    VARIANT_AUTO, VARIANT_CHUNK, VARIANT_TEAM = 0, 1, 2
+
+    def __init__(self, prep, precision=32, device=None, variant=0):
         from . import _native
         torch = _native.require_cuda()
         assert precision in (32, 64)
+        assert 1 <= prep.A <= 8, "the fused kernels support 1 to 8 coupled surfaces"
         self.prep, self.precision = prep, precision
         tabs = prep.tables()
         dt = torch.float32 if precision == 32 else torch.float64
@@ -230,6 +253,7 @@ class DevicePlan:
         m = _native.PbrModel()
         m.A, m.A_rho, m.n_fill_rho, m.N, m.P, m.K = prep.A, prep.A_rho, prep.n_fill_rho, prep.N, prep.P, prep.K
         m.precision = precision
+        m.variant = variant
         m.tau, m.delta_beta, m.log_c0 = prep.tau, prep.delta_beta, tabs["log_c0"]
         for k in self.FIELDS:
             setattr(m, k, self.tensors[k].data_ptr())

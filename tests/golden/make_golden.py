@@ -196,8 +196,14 @@ CASES = {
     "plain": dict(A=2, N=3, P=16, T=300.0, X=50, B=25, model_seed=8, rng_seed=31, pm=False),
     # sampling model with more surfaces than the coupled model (qTempTensor path)
     "arho": dict(A=2, N=3, P=10, T=300.0, X=60, B=30, model_seed=9, rng_seed=55, extra_rho_surfaces=2),
-    # default delta_beta of the reference (2e-4 absolute) instead of 1e-4 beta
+    # one surface
     "single_surface": dict(A=1, N=4, P=8, T=300.0, X=40, B=20, model_seed=3, rng_seed=8),
+    # learned-proposal configuration shapes: A=6, N=20, P=128, T=200 K, strong off-diagonal couplings
+    "cfg4": dict(A=6, N=20, P=128, T=200.0, X=16, B=8, model_seed=44, rng_seed=404, sd_offdiag=0.1),
+    # the largest surface count of the batched configuration
+    "a8": dict(A=8, N=5, P=16, T=400.0, X=24, B=12, model_seed=88, rng_seed=808),
+    # seven surfaces, odd everything
+    "a7": dict(A=7, N=3, P=9, T=150.0, X=21, B=7, model_seed=77, rng_seed=707),
 }
 
 

@@ -18,7 +18,11 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel"]
+CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel",
+         "cfg4", "a8", "a7"]
+WIDE = {"cfg4", "a8", "a7"}                       # A > 4: the row-team form only
+# (case, kernel form): 1 = register-resident chunks, 2 = bead-parallel records + row teams
+FORMS = [(c, v) for c in CASES for v in (1, 2) if not (v == 1 and c in WIDE)]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -29,22 +33,22 @@ def _lib():
     _native.load(build.build())
 
 
-def _eval(c, precision, q=None, want_coef=False):
+def _eval(c, precision, q=None, want_coef=False, variant=0):
     from pibronic_gb300.plan import DevicePlan
     from pibronic_gb300.pimc import evaluate_device
     q = c["q"] if q is None else q
     prep = prepared_from_case(c, q.shape[2])
-    plan = DevicePlan(prep, precision=precision)
+    plan = DevicePlan(prep, precision=precision, variant=variant)
     out = evaluate_device(plan, q.shape[0], q=torch.as_tensor(q, device="cuda"), want_coef=want_coef)
     torch.cuda.synchronize()
     assert int(out["status"].item()) == 0
     return {k: v.cpu().numpy() for k, v in out.items()}
 
 
-@pytest.mark.parametrize("name", CASES)
-def test_fused_fp64_matches_reference(runs, name):
+@pytest.mark.parametrize("name,variant", FORMS)
+def test_fused_fp64_matches_reference(runs, name, variant):
     c = case_of(runs, name)
-    got = _eval(c, 64)
+    got = _eval(c, 64, variant=variant)
     assert np.allclose(got["s_rho"], c["s_rho"], rtol=1e-9, atol=0)
     assert np.allclose(got["s_g"], c["s_g"], rtol=1e-9, atol=0)
     if "s_gP" in c:
@@ -52,10 +56,10 @@ def test_fused_fp64_matches_reference(runs, name):
         assert np.allclose(got["s_gm"], c["s_gM"], rtol=1e-9, atol=0)
 
 
-@pytest.mark.parametrize("name", CASES)
-def test_fused_fp32_matches_reference(runs, name):
+@pytest.mark.parametrize("name,variant", FORMS)
+def test_fused_fp32_matches_reference(runs, name, variant):
     c = case_of(runs, name)
-    got = _eval(c, 32)
+    got = _eval(c, 32, variant=variant)
     assert np.allclose(got["s_rho"], c["s_rho"], rtol=2e-4, atol=0)
     assert np.allclose(got["s_g"], c["s_g"], rtol=2e-4, atol=0)
     if "s_gP" in c:

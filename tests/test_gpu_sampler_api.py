@@ -106,6 +106,20 @@ def test_sampled_q_evaluates_like_oracle(tmp_path):
     assert torch.equal(q2, out["q"])
 
 
+def test_both_kernel_forms_draw_the_same_samples(tmp_path):
+    """The register-chunk and row-team forms consume the same Philox stream: same q, and the
+    same outputs up to FP32 rounding."""
+    from pibronic_gb300.plan import DevicePlan
+    from pibronic_gb300.pimc import evaluate_device
+    FS, data = make_box(tmp_path, A=4, N=12, P=64, X=256)
+    a = evaluate_device(DevicePlan(data.prepared, variant=1), 256, seed=4, offset=77, want_q=True)
+    b = evaluate_device(DevicePlan(data.prepared, variant=2), 256, seed=4, offset=77, want_q=True)
+    assert torch.equal(a["src"], b["src"])
+    assert torch.allclose(a["q"], b["q"], rtol=1e-6, atol=1e-5)
+    for k in ("s_rho", "s_g", "s_gp", "s_gm"):
+        assert torch.allclose(a[k], b[k], rtol=2e-4, atol=0), k
+
+
 def test_counter_based_stream_is_deterministic_and_splittable(tmp_path):
     from pibronic_gb300.pimc import evaluate_device
     FS, data = make_box(tmp_path, A=2, N=3, P=12, X=1000)
@@ -208,12 +222,18 @@ def test_ragged_sample_counts(tmp_path, X):
         assert torch.equal(full[k][:X], part[k])
 
 
-@pytest.mark.parametrize("A,N,P", [(1, 1, 3), (2, 2, 5), (3, 7, 33), (4, 20, 256), (2, 64, 8)])
-def test_shapes_sample_eval_against_oracle(tmp_path, A, N, P):
+SHAPES = [(1, 1, 3), (2, 2, 5), (3, 7, 33), (4, 20, 256), (2, 64, 8), (6, 20, 128), (8, 4, 17),
+          (5, 9, 40)]
+
+
+@pytest.mark.parametrize("A,N,P,variant", [s + (v,) for s in SHAPES for v in (1, 2) if v == 2 or s[0] <= 4])
+def test_shapes_sample_eval_against_oracle(tmp_path, A, N, P, variant):
     from oracle import pimc_oracle as po
+    from pibronic_gb300.plan import DevicePlan
     from pibronic_gb300.pimc import evaluate_device
     FS, data = make_box(tmp_path, A=A, N=N, P=P, X=32, sd_quadratic=0.0005)
-    out = evaluate_device(data.plan, 32, seed=1, offset=0, want_q=True)
+    plan = DevicePlan(data.prepared, precision=32, variant=variant)
+    out = evaluate_device(plan, 32, seed=1, offset=0, want_q=True)
     q = out["q"].double().cpu().numpy()
     box = po.OracleBox(po.model_from_file(FS.path_vib_model),
                        po.model_from_file(FS.path_rho_model, diagonal=True), 32, 32, P,
@@ -251,9 +271,9 @@ def test_errors_are_reported_not_faulted(tmp_path):
     out = evaluate_device(data.plan, 16, q=q)
     assert int(out["status"].item()) == _native.PBR_ERR_NONFINITE
     (tmp_path / "big").mkdir()
-    FS2, data2 = make_box(tmp_path / "big", A=2, N=3, P=300, X=16)
+    FS2, data2 = make_box(tmp_path / "big", A=2, N=65, P=4, X=16, sd_quadratic=0.0)
     with pytest.raises(AssertionError):
-        evaluate_device(data2.plan, 16, seed=1)        # sampling path supports P <= 256
+        evaluate_device(data2.plan, 16, seed=1)        # the fused kernels support N <= 64
     from pibronic_gb300.plan import PreparedModels
     from pibronic_gb300 import vibronic_io
     vib = vibronic_io.load_model_from_JSON(FS.path_vib_model)

@@ -74,7 +74,8 @@ def test_explicit_block_compute(ex_box, explicit):
     assert np.allclose(g_all, explicit["numerator_g"], rtol=RTOL, atol=ATOL)
 
 
-CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel"]
+CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel",
+         "cfg4", "a8", "a7"]
 
 
 @pytest.mark.parametrize("name", CASES)
