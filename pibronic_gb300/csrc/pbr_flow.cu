@@ -322,7 +322,7 @@ __global__ void gemm_tn_reduce(const float* __restrict__ part, int splits, int M
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MN; i += gridDim.x * blockDim.x) {
         float acc = 0.f;
         for (int s = 0; s < splits; ++s) acc += part[static_cast<int64_t>(s) * MN + i];
-        C[i] = beta * C[i] + acc;
+        C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
     }
 }
 
@@ -437,7 +437,8 @@ int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t ns
                      const double* inv_sigma, const double* rho_csch, const double* rho_tanh2, float* y,
                      double* U, void* stream) {
     if (!q || !center || !inv_sigma || !rho_csch || !rho_tanh2 || !y || !U) return PBR_ERR_ARG;
-    if (X < 0 || N < 1 || P < 3 || nsel < 1 || nsel > 8 || nsel > P) return PBR_ERR_ARG;
+    // slots beyond the cos/sin pairs (the alternating mode of an even ring) are not supported
+    if (X < 0 || N < 1 || P < 3 || nsel < 1 || nsel > 8 || nsel > 1 + 2 * ((P - 1) / 2)) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int threads = 128;
     flow_prepare_kernel<<<grid_for(X * 32, threads), threads, 0, static_cast<cudaStream_t>(stream)>>>(
@@ -447,7 +448,9 @@ int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t ns
 
 int pbr_flow_apply(const float* q, const float* y, const float* y_new, int64_t X, int32_t N, int32_t P,
                    int32_t nsel, const double* sigma, float* x, void* stream) {
-    if (!q || !y || !y_new || !sigma || !x || X < 0 || N < 1 || P < 3 || nsel < 1) return PBR_ERR_ARG;
+    if (!q || !y || !y_new || !sigma || !x || X < 0 || N < 1 || P < 3 || nsel < 1 || nsel > 8 ||
+        nsel > 1 + 2 * ((P - 1) / 2))
+        return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     flow_apply_kernel<<<grid_for(X * N * P, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         q, y, y_new, X, N, P, nsel, sigma, x);
