@@ -272,8 +272,10 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     hist = torch.empty((args.steps + args.warmup, 12), dtype=torch.float64, device=dev)
 
+    from pibronic_gb300.shard import allgather_moments, counter_offset
+
     def step(i, e_k0=None, e_k1=None):
-        offset = (i * world + rank) * X
+        offset = counter_offset(i, rank, world, X)
         if e_k0 is not None:
             e_k0.record(stream)
         _native.check(lib.pbr_sample_eval(plan.struct, data.seed, offset, X, o, sh), "sample_eval")
@@ -310,16 +312,15 @@ def run_ours(args):
         raise RuntimeError("non-finite results in the timed steps")
     H = hist.cpu().numpy()[args.warmup:]
     ests = [stats.estimates_from_moments(h[:7], h[7:], T_) for h in H]
-    ess = statistics.mean(e["ESS"] for e in ests)
-    t = torch.tensor([ms_step, ess, ms_kern], dtype=torch.float64, device=dev)
     if dist:
-        tmax = t.clone()
-        dist.all_reduce(tmax[:1], op=dist.ReduceOp.MAX)
-        tsum = t.clone()
-        dist.all_reduce(tsum[1:2])
-        ms_step, ess_total = float(tmax[0]), float(tsum[1])
+        # per step, the ESS of all ranks' samples together: merge the moments in rank order
+        ess_total = statistics.mean(
+            stats.estimates_from_moments(allgather_moments(h[:7]), None, T_)["ESS"] for h in H)
+        tmax = torch.tensor([ms_step], dtype=torch.float64, device=dev)
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        ms_step = float(tmax[0])
     else:
-        ess_total = ess
+        ess_total = statistics.mean(e["ESS"] for e in ests)
     value = ess_total / (ms_step * 1e-3)
     sps = X * world / (ms_step * 1e-3)
     e = ests[-1]
@@ -339,7 +340,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         for k, v in tab_host.items():                 # the step's inputs: model tables
             plan.tensors[k].copy_(v, non_blocking=True)
-        _native.check(lib.pbr_sample_eval(plan.struct, data.seed + 1, (s * world + rank) * X, X, o, sh),
+        _native.check(lib.pbr_sample_eval(plan.struct, data.seed + 1, counter_offset(s, rank, world, X), X, o, sh),
                       "sample_eval")
         red.launch(bufs["s_rho"], bufs["s_g"], bufs["s_gp"], bufs["s_gm"], data.delta_beta, T_, stream)
         for k in bufs:
@@ -379,6 +380,12 @@ def run_ours(args):
                 "ms_per_step": 1e3 * e2e_t},
         "clocks": clk, "gpu_launches": 5 * args.steps,
     }
+    # ---- learned proposal vs plain rho (A=6, N=20, P=128, T=200 K, strong couplings) ----
+    if rank == 0 and not args.no_learned:
+        line["learned"] = learned_leg(args)
+    # ---- batched uneven models in one graph-captured launch per surface count ----
+    if rank == 0 and not args.no_batched:
+        line["batched"] = batched_leg(args)
     # ---- CPU baseline: the oracle port on the host cores, rank 0 at N=1 only ----
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
@@ -395,6 +402,103 @@ def run_ours(args):
     return 0
 
 
+def _timed(torch, fn):
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return r, time.perf_counter() - t0
+
+
+def learned_leg(args):
+    """The learned-proposal configuration: plain rho vs the affine-coupling flow trained on 2e6 of
+    rho's own weighted samples plus one round on its own samples; ESS/s includes the flow's
+    sampling and evaluation, training time is reported separately."""
+    import torch
+    from pibronic_gb300 import constants, pimc, stats, synthetic
+    from pibronic_gb300.file_structure import FileStructure
+    from pibronic_gb300.flow import FlowProposal
+    from pibronic_gb300.pimc import evaluate_device
+    A, N, P, T = 6, 20, 128, 200.0
+    X = args.learned_samples
+    out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K off-diagonal couplings N(0,0.1) eV, dbeta=1e-4 beta, "
+                       f"{X} samples per evaluation; flow: 8 coupling layers, hidden 128, 3 ring slots per mode",
+           "models": []}
+    for seed in args.learned_seeds:
+        root = tempfile.mkdtemp(prefix="pbr_learned_")
+        FS = FileStructure(root, 0, 0)
+        synthetic.write_model_pair(FS, A, N, seed, sd_offdiag=0.1)
+        data = pimc.BoxDataPM(1e-4 * constants.beta(T))
+        data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+        data.states, data.modes, data.beads, data.temperature = A, N, P, T
+        data.samples = data.block_size = 1000
+        data.blocks = 1
+        data.preprocess()
+        evaluate_device(data.plan, 10_000, seed=99, offset=0)
+        plain, tp = _timed(torch, lambda: evaluate_device(data.plan, X, seed=1, offset=0, want_q=True))
+        ep = stats.device_estimates(plain["s_rho"], plain["s_g"], plain["s_gp"], plain["s_gm"], T, data.delta_beta)
+        fl = FlowProposal(data.prepared, data.plan, nsel=3, layers=8, hidden=128, seed=0)
+        ys, rs = [], []
+        for k, pl in enumerate((plain, evaluate_device(data.plan, X, seed=1, offset=X, want_q=True))):
+            y, _ = fl.prepare(pl["q"])
+            ys.append(y)
+            rs.append(pl["s_g"] / pl["s_rho"])
+            del pl["q"]
+        _, t_train = _timed(torch, lambda: fl.train(torch.cat(ys), torch.cat(rs), epochs=6, batch=16384, lr=1e-3))
+        first = fl.sample_and_evaluate(X, seed=7, keep=True)
+        _, t2 = _timed(torch, lambda: fl.train(first["y"], first["s_g"] / first["s_q"], epochs=6, batch=16384,
+                                               lr=1e-3))
+        del first
+        fl.sample_and_evaluate(10_000, seed=5)
+        res, tf = _timed(torch, lambda: fl.sample_and_evaluate(X, seed=8))
+        ef = stats.device_estimates(res["s_q"], res["s_g"], res["s_gp"], res["s_gm"], T, data.delta_beta)
+
+        def summary(e, t):
+            rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
+                   "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
+            sps = X / t
+            return {"ess_per_sample": e["ESS"] / X, "ess_per_s": e["ESS"] / t, "samples_per_s": sps,
+                    "Z": e["Z"], "Z error": e["Z error"], "E": e["jk_E"], "E error": e["jk_E error"],
+                    "Cv": e["jk_Cv"], "Cv error": e["jk_Cv error"],
+                    "time_to_1e-3_s": {k: X * (v / 1e-3) ** 2 / sps for k, v in rel.items()}}
+        sp, sl = summary(ep, tp), summary(ef, tf)
+        agree = {k: abs(sl[k] - sp[k]) / math.hypot(sl[k + " error"], sp[k + " error"]) for k in ("Z", "E", "Cv")}
+        out["models"].append({"model_seed": seed, "plain": sp, "learned": sl, "train_s": t_train + t2,
+                              "ess_per_s_ratio": sl["ess_per_s"] / sp["ess_per_s"],
+                              "wall_to_1e-3_ratio": max(sp["time_to_1e-3_s"].values()) / max(sl["time_to_1e-3_s"].values()),
+                              "agreement_sigma": agree})
+    out["median_ess_per_s_ratio"] = statistics.median(m["ess_per_s_ratio"] for m in out["models"])
+    return out
+
+
+def batched_leg(args):
+    """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
+    each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
+    import torch
+    from pibronic_gb300 import synthetic
+    from pibronic_gb300.batch import ModelBatch, autotune
+    count, X = args.batch_models, args.batch_samples
+    preps = synthetic.batch_models(count=count, seed=3)
+    seeds = list(range(1, count + 1))
+    budget, times = autotune(preps, seeds, X_probe=2048)
+    mb = ModelBatch(preps, [X] * count, seeds, smem_budget=budget)
+    mb.capture()
+    mb.replay()
+    ts = []
+    for _ in range(3):
+        _, t = _timed(torch, mb.replay)
+        ts.append(t)
+    t = min(ts)
+    ests = mb.estimates()
+    W = sum(flops_per_sample(p.A, p.N, p.P) for p in preps) * X
+    return {"workload": f"{count} models, A~U{{2..8}}, N~U{{3..20}}, P~U{{8..256}}, T~U[100,500]K, {X} samples each",
+            "samples_per_s": count * X / t, "ms_per_pass": 1e3 * t, "launch_groups": mb.groups,
+            "smem_budget_bytes": budget, "autotune_ms": {str(k): 1e3 * v for k, v in times.items()},
+            "algorithmic_tflops": W / t / 1e12,
+            "median_ess_per_sample": statistics.median(e["ESS"] / X for e in ests),
+            "finite": bool(int(mb.status.item()) == 0)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,6 +509,12 @@ def main():
     ap.add_argument("--cpu-samples", type=int, default=400, help="samples per host process (CPU legs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=0, help="fused-kernel form: 0 auto, 1 chunks, 2 teams")
+    ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--learned-samples", type=int, default=1_000_000)
+    ap.add_argument("--learned-seeds", type=int, nargs="+", default=[404, 44, 4])
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-models", type=int, default=256)
+    ap.add_argument("--batch-samples", type=int, default=100_000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -119,6 +119,23 @@ int pbr_sample_eval(const pbr_model* model, uint64_t seed, uint64_t offset, int6
                     const pbr_outputs* out, void* stream);
 
 /*
+ * Many independent models in one launch per surface count (the batched configuration): every
+ * model keeps its own sizes, temperature, seed, counter offset and outputs.  pbr_batch_pack fills
+ * a host blob of pbr_batch_blob_bytes(n) bytes (tile shapes per model within smem_budget bytes of
+ * shared memory, 0 = the maximum; models grouped by surface count and series order; grid_cap
+ * limits the persistent grid, 0 = occupancy x SMs); the caller copies it to a device buffer of the
+ * same size; pbr_sample_eval_batch launches one persistent row-team kernel per group, CTAs taking
+ * the concatenated tiles round-robin.  All models need precision 32.  The launches can be captured
+ * in a CUDA graph (the blob holds everything they read).
+ */
+int64_t pbr_batch_blob_bytes(int32_t n_models);
+int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_t* offsets, const int64_t* X,
+                   const pbr_outputs* outs, int32_t n_models, int32_t smem_budget, int32_t grid_cap,
+                   void* host_blob);
+int pbr_sample_eval_batch(const void* host_blob, const void* device_blob, void* stream);
+int32_t pbr_batch_groups(const void* host_blob);
+
+/*
  * Sampling only: the bead coordinates q [X * N * P] (FP32) and source surfaces src [X]
  * (nullable) that pbr_sample_eval draws for the same seed and offset.
  * Replaces draw_sample + transform_sampled_coordinates (pimc.py:326-334, 613-631).
@@ -204,6 +221,20 @@ int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
 int pbr_reduce_jackknife(const double* s_rho, const double* s_g, const double* s_gp,
                          const double* s_gm, int64_t X, double delta_beta, double kB_T2,
                          const double* totals, double* scratch, double* out, void* stream);
+
+/*
+ * Segmented forms for batched launches: M independent reductions over s_*[seg[m] .. seg[m+1])
+ * (seg: M+1 int64, device), each with its own delta_beta[m] (and kB T^2 [m]); moments [M][7] and
+ * out [M][5] in the layouts above; the jackknife pass takes the moments of the first.  scratch
+ * holds pbr_reduce_segments_scratch(M) doubles.  M <= 65535.
+ */
+int pbr_reduce_terms_segments(const double* s_rho, const double* s_g, const double* s_gp, const double* s_gm,
+                              const int64_t* seg, int32_t M, const double* delta_beta, double* scratch,
+                              double* moments, void* stream);
+int pbr_reduce_jackknife_segments(const double* s_rho, const double* s_g, const double* s_gp, const double* s_gm,
+                                  const int64_t* seg, int32_t M, const double* delta_beta, const double* kB_T2,
+                                  const double* moments, double* scratch, double* out, void* stream);
+int64_t pbr_reduce_segments_scratch(int32_t M);
 
 /* Number of partial blocks the reductions use for X samples. */
 int64_t pbr_reduce_blocks(int64_t X);
@@ -306,6 +337,18 @@ int pbr_flow_weights(const double* lse_y, const double* U, const double* logdet,
 /* Adam step (bias-corrected with the 1-based step). */
 int pbr_adam(float* param, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
              float beta2, float eps, int32_t step, void* stream);
+
+/*
+ * 5th-generation tensor-core GEMM (tcgen05.mma into TMEM, operands staged in shared memory in the
+ * no-swizzle K-major core-matrix layout, completion through an mbarrier, tcgen05.ld epilogue):
+ * C [M][N] FP32 = A [M][K] B [N][K]^T with fmt 1 = BF16 or 2 = TF32 (FP32 storage) operands,
+ * M % 128 == 0, N % 16 == 0 and 16 <= N <= 256, K a multiple of 64 (BF16) or 32 (TF32), A and B
+ * 16-byte aligned.  Waits are bounded: a CTA that times out writes PBR_ERR_CUDA to *status
+ * (nullable) and frees its tensor memory.  No counterpart in the reference (the contraction the
+ * reference does with numpy einsum, pimc.py:1147, at large N).
+ */
+int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K,
+                int32_t* status, void* stream);
 
 /* Library version string and the SM architecture it was built for. */
 const char* pbr_version(void);

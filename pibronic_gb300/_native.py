@@ -31,7 +31,9 @@ EXPORTED = (
     "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples",
     "pbr_flow_prepare", "pbr_flow_apply", "pbr_flow_layer_forward", "pbr_flow_layer_backward",
     "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
-    "pbr_adam", "pbr_version",
+    "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
+    "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
+    "pbr_tc_gemm", "pbr_version",
 )
 
 
@@ -107,6 +109,14 @@ def _declare(lib):
         "pbr_flow_base": (C.c_int, [vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "pbr_flow_weights": (C.c_int, [vp, vp, vp, vp, i64, vp, vp]),
         "pbr_adam": (C.c_int, [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]),
+        "pbr_batch_blob_bytes": (i64, [i32]),
+        "pbr_batch_pack": (C.c_int, [vp, vp, vp, vp, vp, i32, i32, i32, vp]),
+        "pbr_sample_eval_batch": (C.c_int, [vp, vp, vp]),
+        "pbr_batch_groups": (i32, [vp]),
+        "pbr_reduce_terms_segments": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]),
+        "pbr_reduce_jackknife_segments": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]),
+        "pbr_reduce_segments_scratch": (i64, [i32]),
+        "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

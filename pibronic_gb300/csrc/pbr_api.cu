@@ -7,6 +7,7 @@
 namespace pbr {
 template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
 template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
+template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, cudaStream_t);
 }
 
 namespace {
@@ -25,10 +26,12 @@ int ilog2(int x) {
     return l;
 }
 
-int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
-             uint64_t offset, const pbr_outputs* out, cudaStream_t st) {
+// Tile shape of the row-team form for one model: S samples per tile (as many as 256 threads
+// hold, halved until the shared memory fits the budget), G teams per sample, C beads per team.
+int make_team_args(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
+                   uint64_t offset, const pbr_outputs* out, int smem_budget, pbr::TeamArgs* pa) {
     using namespace pbr;
-    TeamArgs a;
+    TeamArgs& a = *pa;
     std::memset(&a, 0, sizeof(a));
     a.m = m;
     a.q_in = q_in;
@@ -49,11 +52,26 @@ int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_
         a.G = 1;
         while (a.G * 2 <= max_teams / a.S && a.G * 2 <= m.P) a.G *= 2;
         const TeamPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.G, a.qstride, a.rl);
-        if (plan.total_bytes <= kMaxSmem) break;
+        if (plan.total_bytes <= smem_budget) break;
         if (a.S == 1) return PBR_ERR_UNSUPPORTED;
         a.S = std::max(1, a.S / 2);
     }
     a.C = (m.P + a.G - 1) / a.G;
+    return PBR_OK;
+}
+
+int team_smem(const pbr::TeamArgs& a, int qmode) {
+    const pbr::TeamPlan plan(a.m.A, a.m.K, qmode, a.m.precision == 32 ? 4 : 8, a.m.N, a.m.P, a.S, a.G,
+                             a.qstride, a.rl);
+    return plan.total_bytes;
+}
+
+int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
+             uint64_t offset, const pbr_outputs* out, cudaStream_t st) {
+    using namespace pbr;
+    TeamArgs a;
+    const int rc = make_team_args(m, qmode, q_in, X, seed, offset, out, kMaxSmem, &a);
+    if (rc != PBR_OK) return rc;
     switch (m.A) {
         case 1: return launch_team<1>(m.K, qmode, m.precision, a, st);
         case 2: return launch_team<2>(m.K, qmode, m.precision, a, st);
@@ -197,6 +215,99 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
     };
     if (m.precision == 32) return go(sample_q_kernel<float>);
     return go(sample_q_kernel<double>);
+}
+
+// ---- batched multi-model launch ------------------------------------------------------------
+namespace {
+constexpr int kBatchMaxGroups = 16;
+struct BatchGroup {
+    int32_t A, K, n_items, smem_bytes;
+    int64_t first_item, total_tiles;
+};
+struct BatchHeader {
+    int32_t n_groups, n_items, grid_cap, pad;
+    BatchGroup groups[kBatchMaxGroups];
+};
+}  // namespace
+
+int64_t pbr_batch_blob_bytes(int32_t n_models) {
+    return static_cast<int64_t>(sizeof(BatchHeader)) + static_cast<int64_t>(n_models) * sizeof(pbr::TeamBatchItem);
+}
+
+int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_t* offsets, const int64_t* X,
+                   const pbr_outputs* outs, int32_t n_models, int32_t smem_budget, int32_t grid_cap,
+                   void* host_blob) {
+    using namespace pbr;
+    if (!models || !seeds || !offsets || !X || !outs || !host_blob || n_models < 1) return PBR_ERR_ARG;
+    const int budget = (smem_budget > 0 && smem_budget < kMaxSmem) ? smem_budget : kMaxSmem;
+    auto* hdr = static_cast<BatchHeader*>(host_blob);
+    auto* items = reinterpret_cast<TeamBatchItem*>(hdr + 1);
+    std::memset(hdr, 0, sizeof(BatchHeader));
+    hdr->grid_cap = grid_cap;
+    int n = 0;
+    // group by (A, K) in increasing A; within a group keep the caller's order
+    for (int A = 1; A <= PBR_MAX_A; ++A)
+        for (int K = 0; K <= 4; K += 4) {
+            const int first = n;
+            int64_t tiles = 0;
+            int smem = 0;
+            for (int i = 0; i < n_models; ++i) {
+                const pbr_model& m = models[i];
+                if (m.A != A || m.K != K) continue;
+                if (m.precision != 32 || m.A_rho < m.A || m.n_fill_rho != m.A || m.N < 1 ||
+                    m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P || X[i] < 0 || !outs[i].s_rho || !outs[i].s_g ||
+                    (K > 0 && (!outs[i].s_gp || !outs[i].s_gm)) || !m.ring_chol || !m.src_cdf)
+                    return PBR_ERR_ARG;
+                TeamBatchItem& it = items[n];
+                const int rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], budget, &it.a);
+                if (rc != PBR_OK) return rc;
+                it.tile_begin = tiles;
+                tiles += (X[i] + it.a.S - 1) / it.a.S;
+                smem = std::max(smem, team_smem(it.a, kSample));
+                ++n;
+            }
+            if (n > first) {
+                if (hdr->n_groups >= kBatchMaxGroups) return PBR_ERR_UNSUPPORTED;
+                BatchGroup& g = hdr->groups[hdr->n_groups++];
+                g.A = A; g.K = K; g.n_items = n - first; g.smem_bytes = smem;
+                g.first_item = first; g.total_tiles = tiles;
+            }
+        }
+    if (n != n_models) return PBR_ERR_ARG;
+    hdr->n_items = n;
+    return PBR_OK;
+}
+
+int pbr_sample_eval_batch(const void* host_blob, const void* device_blob, void* stream) {
+    using namespace pbr;
+    if (!host_blob || !device_blob) return PBR_ERR_ARG;
+    const auto* hdr = static_cast<const BatchHeader*>(host_blob);
+    const auto* items = reinterpret_cast<const TeamBatchItem*>(
+        static_cast<const char*>(device_blob) + sizeof(BatchHeader));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int gi = 0; gi < hdr->n_groups; ++gi) {
+        const BatchGroup& g = hdr->groups[gi];
+        if (g.total_tiles == 0) continue;
+        const TeamBatchItem* gitems = items + g.first_item;
+        int rc = PBR_ERR_UNSUPPORTED;
+        switch (g.A) {
+            case 1: rc = launch_team_batch<1>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 2: rc = launch_team_batch<2>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 3: rc = launch_team_batch<3>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 4: rc = launch_team_batch<4>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 5: rc = launch_team_batch<5>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 6: rc = launch_team_batch<6>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 7: rc = launch_team_batch<7>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 8: rc = launch_team_batch<8>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            default: break;
+        }
+        if (rc != PBR_OK) return rc;
+    }
+    return PBR_OK;
+}
+
+int32_t pbr_batch_groups(const void* host_blob) {
+    return host_blob ? static_cast<const BatchHeader*>(host_blob)->n_groups : 0;
 }
 
 const char* pbr_version(void) { return "pibronic_gb300 0.1 sm_103a"; }

@@ -23,6 +23,8 @@ namespace {
 constexpr int kFlowWarps = 4;
 constexpr float kKappa = 2.0f;
 
+__host__ __device__ inline int align_up_(int x, int a) { return (x + a - 1) / a * a; }
+
 inline int sm_count() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -40,51 +42,54 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
                                     const double* __restrict__ center, const double* __restrict__ inv_sigma,
                                     const double* __restrict__ rho_csch, const double* __restrict__ rho_tanh2,
                                     float* __restrict__ y, double* __restrict__ U) {
+    extern __shared__ float basis[];            // [nsel][P] ring basis columns, FP32
+    const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
+    const double amp = sqrt(2.0 / P);
+    for (int i = threadIdx.x; i < nsel * P; i += blockDim.x) {
+        const int s = i / P, p = i - s * P;
+        double bv = inv_sqrt_p;
+        if (s > 0) {
+            double sn, cs;
+            sincospi(2.0 * ((s + 1) / 2) * p / P, &sn, &cs);
+            bv = amp * ((s & 1) ? cs : sn);
+        }
+        basis[i] = static_cast<float>(bv);
+    }
+    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t gw = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
     const int64_t nw = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-    const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
-    const double amp = sqrt(2.0 / P);
     for (int64_t x = gw; x < X; x += nw) {
         double quad_total = 0.0, ysq = 0.0;
         for (int j = 0; j < N; ++j) {
             const float* qj = q + (x * N + j) * static_cast<int64_t>(P);
-            const double c = center[j];
-            double quad = 0.0;
-            double proj[8];
+            const float c = static_cast<float>(center[j]);
+            const float ch = static_cast<float>(rho_csch[j]), th2 = static_cast<float>(2.0 * rho_tanh2[j]);
+            float quad = 0.0f;
+            float proj[8];
 #pragma unroll
-            for (int s = 0; s < 8; ++s) proj[s] = 0.0;
+            for (int s = 0; s < 8; ++s) proj[s] = 0.0f;
             for (int p = lane; p < P; p += 32) {
-                const double xp = static_cast<double>(qj[p]) - c;
-                const double xn = static_cast<double>(qj[(p + 1 == P) ? 0 : p + 1]) - c;
-                const double d = xp - xn;
-                quad += rho_csch[j] * d * d + 2.0 * rho_tanh2[j] * xp * xp;
+                const float xp = qj[p] - c;
+                const float xn = qj[(p + 1 == P) ? 0 : p + 1] - c;
+                const float d = xp - xn;
+                quad = fmaf(ch * d, d, fmaf(th2 * xp, xp, quad));
 #pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    if (s >= nsel) break;
-                    double bv;
-                    if (s == 0) {
-                        bv = inv_sqrt_p;
-                    } else {
-                        const int k = (s + 1) / 2;
-                        double sn, cs;
-                        sincospi(2.0 * k * p / P, &sn, &cs);
-                        bv = amp * ((s & 1) ? cs : sn);
-                    }
-                    proj[s] += bv * xp;
-                }
+                for (int s = 0; s < 8; ++s)
+                    if (s < nsel) proj[s] = fmaf(basis[s * P + p], xp, proj[s]);
             }
+            double qd = static_cast<double>(quad);
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) {
-                quad += __shfl_xor_sync(0xffffffffu, quad, o);
+                qd += __shfl_xor_sync(0xffffffffu, qd, o);
 #pragma unroll
                 for (int s = 0; s < 8; ++s) proj[s] += __shfl_xor_sync(0xffffffffu, proj[s], o);
             }
-            quad_total += quad;
+            quad_total += qd;
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 if (s >= nsel) break;
-                const double v = proj[s] * inv_sigma[j * nsel + s];
+                const double v = static_cast<double>(proj[s]) * inv_sigma[j * nsel + s];
                 ysq += v * v;
                 if (lane == 0) y[x * static_cast<int64_t>(N * nsel) + j * nsel + s] = static_cast<float>(v);
             }
@@ -97,30 +102,32 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
 __global__ void flow_apply_kernel(const float* __restrict__ q, const float* __restrict__ y,
                                   const float* __restrict__ yn, int64_t X, int N, int P, int nsel,
                                   const double* __restrict__ sigma, float* __restrict__ xo) {
-    const int64_t total = X * N * static_cast<int64_t>(P);
+    extern __shared__ float basis[];            // [nsel][P]
     const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
     const double amp = sqrt(2.0 / P);
+    for (int i = threadIdx.x; i < nsel * P; i += blockDim.x) {
+        const int s = i / P, p = i - s * P;
+        double bv = inv_sqrt_p;
+        if (s > 0) {
+            double sn, cs;
+            sincospi(2.0 * ((s + 1) / 2) * p / P, &sn, &cs);
+            bv = amp * ((s & 1) ? cs : sn);
+        }
+        basis[i] = static_cast<float>(bv);
+    }
+    __syncthreads();
+    const int64_t total = X * N * static_cast<int64_t>(P);
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int p = static_cast<int>(i % P);
         const int64_t xj = i / P;
         const int j = static_cast<int>(xj % N);
         const int64_t x = xj / N;
-        double acc = q[i];
-        for (int s = 0; s < nsel; ++s) {
-            double bv;
-            if (s == 0) {
-                bv = inv_sqrt_p;
-            } else {
-                const int k = (s + 1) / 2;
-                double sn, cs;
-                sincospi(2.0 * k * p / P, &sn, &cs);
-                bv = amp * ((s & 1) ? cs : sn);
-            }
-            const int64_t yi = x * static_cast<int64_t>(N * nsel) + j * nsel + s;
-            acc += bv * sigma[j * nsel + s] * (static_cast<double>(yn[yi]) - static_cast<double>(y[yi]));
-        }
-        xo[i] = static_cast<float>(acc);
+        float acc = q[i];
+        const int64_t y0 = x * static_cast<int64_t>(N * nsel) + j * nsel;
+        for (int s = 0; s < nsel; ++s)
+            acc = fmaf(basis[s * P + p] * static_cast<float>(sigma[j * nsel + s]), yn[y0 + s] - y[y0 + s], acc);
+        xo[i] = acc;
     }
 }
 
@@ -145,17 +152,37 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// UPH consecutive floats from shared memory (UPH in {1, 2, 4, 8}), vector loads
+template <int UPH>
+__device__ __forceinline__ void ldu(const float* __restrict__ p, float (&v)[UPH]) {
+    if constexpr (UPH % 4 == 0) {
+#pragma unroll
+        for (int u = 0; u < UPH; u += 4) {
+            const float4 t = *reinterpret_cast<const float4*>(p + u);
+            v[u] = t.x; v[u + 1] = t.y; v[u + 2] = t.z; v[u + 3] = t.w;
+        }
+    } else if constexpr (UPH == 2) {
+        const float2 t = *reinterpret_cast<const float2*>(p);
+        v[0] = t.x; v[1] = t.y;
+    } else {
+        v[0] = p[0];
+    }
+}
+
+// Layer in either direction.  Lane l owns hidden units [l*UPH, (l+1)*UPH); the output head
+// pairs (s_j, t_j) belong to lane j mod 32; k-sums are split in four interleaved partials.
+template <int UPH>
 __global__ void flow_layer_fwd_kernel(const LayerDev L, int dir, int64_t X, float* __restrict__ y,
                                       double* __restrict__ logdet, const SaveDev sv) {
     extern __shared__ __align__(16) float fsm[];
     const int I = L.I, J = L.J, H = L.H, D = L.D, O = 2 * J;
-    float* w1 = fsm;
-    float* w2 = w1 + I * H;
-    float* w3 = w2 + H * H;
+    float* w1 = fsm;                       // [I][H]
+    float* w2 = w1 + I * H;                // [H][H]
+    float* w3 = w2 + H * H;                // [H][O]
     float* bb1 = w3 + H * O;
     float* bb2 = bb1 + H;
     float* bb3 = bb2 + H;
-    float* wbuf = bb3 + O;
+    float* wbuf = bb3 + align_up_(O, 4);
     for (int i = threadIdx.x; i < I * H; i += blockDim.x) w1[i] = L.W1[i];
     for (int i = threadIdx.x; i < H * H; i += blockDim.x) w2[i] = L.W2[i];
     for (int i = threadIdx.x; i < H * O; i += blockDim.x) w3[i] = L.W3[i];
@@ -163,41 +190,67 @@ __global__ void flow_layer_fwd_kernel(const LayerDev L, int dir, int64_t X, floa
     for (int i = threadIdx.x; i < O; i += blockDim.x) bb3[i] = L.b3[i];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* ya = wbuf + warp * (I + 2 * H);
-    float* h1 = ya + I;
+    const int WB = align_up_(I, 4) + 2 * H;
+    float* ya = wbuf + warp * WB;
+    float* h1 = ya + align_up_(I, 4);
     float* h2 = h1 + H;
+    const int h0 = lane * UPH;
     const int64_t nw = static_cast<int64_t>(gridDim.x) * kFlowWarps;
     for (int64_t x = static_cast<int64_t>(blockIdx.x) * kFlowWarps + warp; x < X; x += nw) {
         float* yx = y + x * D;
         for (int i = lane; i < I; i += 32) ya[i] = yx[L.idx_a[i]];
         __syncwarp();
-        for (int h = lane; h < H; h += 32) {
-            float z = bb1[h];
-            for (int i = 0; i < I; ++i) z = fmaf(ya[i], w1[i * H + h], z);
-            h1[h] = tanhf(z);
+        {
+            float acc[UPH], w[UPH];
+            ldu<UPH>(bb1 + h0, acc);
+            for (int i = 0; i < I; ++i) {
+                const float a = ya[i];
+                ldu<UPH>(w1 + i * H + h0, w);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[u] = fmaf(a, w[u], acc[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) h1[h0 + u] = tanhf(acc[u]);
         }
         __syncwarp();
-        for (int h = lane; h < H; h += 32) {
-            float z = bb2[h];
-            for (int k = 0; k < H; ++k) z = fmaf(h1[k], w2[k * H + h], z);
-            h2[h] = tanhf(z);
+        {
+            float acc[2][UPH], w[UPH];
+            ldu<UPH>(bb2 + h0, acc[0]);
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) acc[1][u] = 0.f;
+            for (int k = 0; k < H; k += 2) {
+                const float a0 = h1[k], a1 = h1[k + 1];
+                ldu<UPH>(w2 + k * H + h0, w);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[0][u] = fmaf(a0, w[u], acc[0][u]);
+                ldu<UPH>(w2 + (k + 1) * H + h0, w);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[1][u] = fmaf(a1, w[u], acc[1][u]);
+            }
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) h2[h0 + u] = tanhf(acc[0][u] + acc[1][u]);
         }
         __syncwarp();
         float ssum = 0.0f;
         for (int j = lane; j < J; j += 32) {
-            float os = bb3[j], ot = bb3[J + j];
-            for (int k = 0; k < H; ++k) {
-                const float hk = h2[k];
-                os = fmaf(hk, w3[k * O + j], os);
-                ot = fmaf(hk, w3[k * O + J + j], ot);
+            float os[4] = {bb3[j], 0.f, 0.f, 0.f}, ot[4] = {bb3[J + j], 0.f, 0.f, 0.f};
+            for (int k = 0; k < H; k += 4) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const float hk = h2[k + u];
+                    os[u] = fmaf(hk, w3[(k + u) * O + j], os[u]);
+                    ot[u] = fmaf(hk, w3[(k + u) * O + J + j], ot[u]);
+                }
             }
-            const float s = kKappa * tanhf(os / kKappa);
+            const float so = (os[0] + os[1]) + (os[2] + os[3]);
+            const float to = (ot[0] + ot[1]) + (ot[2] + ot[3]);
+            const float sv_s = kKappa * tanhf(so / kKappa);
             const int bi = L.idx_b[j];
             const float yb = yx[bi];
-            const float out = (dir > 0) ? fmaf(yb, __expf(s), ot) : (yb - ot) * __expf(-s);
+            const float out = (dir > 0) ? fmaf(yb, __expf(sv_s), to) : (yb - to) * __expf(-sv_s);
             yx[bi] = out;
-            ssum += s;
-            if (sv.s) { sv.s[x * J + j] = s; sv.yb[x * J + j] = out; }
+            ssum += sv_s;
+            if (sv.s) { sv.s[x * J + j] = sv_s; sv.yb[x * J + j] = out; }
         }
         ssum = warp_sum(ssum);
         if (lane == 0) logdet[x] += (dir > 0) ? static_cast<double>(ssum) : -static_cast<double>(ssum);
@@ -212,19 +265,21 @@ __global__ void flow_layer_fwd_kernel(const LayerDev L, int dir, int64_t X, floa
 // Back-propagation through one layer of the inverse direction.  gy holds dL/dy of the layer's
 // output on entry and dL/dy' of its input on exit; g_o [X][2J], g_z2 / g_z1 [X][H] are written
 // for the weight-gradient GEMMs.  rt[x] is the sample's normalised weight (the log-det term).
+template <int UPH>
 __global__ void flow_layer_bwd_kernel(const LayerDev L, int64_t X, float* __restrict__ gy,
                                       const float* __restrict__ rt, const SaveDev sv,
                                       float* __restrict__ g_o, float* __restrict__ g_z2,
                                       float* __restrict__ g_z1) {
     extern __shared__ __align__(16) float fsm[];
     const int I = L.I, J = L.J, H = L.H, D = L.D, O = 2 * J;
-    float* w1t = fsm;                 // [H][I]
-    float* w2t = w1t + H * I;         // [H][H]  (transposed)
-    float* w3t = w2t + H * H;         // [O][H]
+    const int IP = align_up_(I, 32);
+    float* w1t = fsm;                 // [H][IP]  W1 transposed
+    float* w2t = w1t + H * IP;        // [H][H]   W2 transposed
+    float* w3t = w2t + H * H;         // [O][H]   W3 transposed
     float* wbuf = w3t + O * H;
-    for (int i = threadIdx.x; i < I * H; i += blockDim.x) {
-        const int r = i / H, c = i - r * H;
-        w1t[c * I + r] = L.W1[i];
+    for (int i = threadIdx.x; i < H * IP; i += blockDim.x) {
+        const int k = i / IP, r = i - k * IP;
+        w1t[i] = (r < I) ? L.W1[r * H + k] : 0.f;
     }
     for (int i = threadIdx.x; i < H * H; i += blockDim.x) {
         const int r = i / H, c = i - r * H;
@@ -236,9 +291,11 @@ __global__ void flow_layer_bwd_kernel(const LayerDev L, int64_t X, float* __rest
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    float* go = wbuf + warp * (O + 2 * H);
-    float* gz2 = go + O;
+    const int WB = align_up_(O, 4) + 2 * H;
+    float* go = wbuf + warp * WB;
+    float* gz2 = go + align_up_(O, 4);
     float* gz1 = gz2 + H;
+    const int h0 = lane * UPH;
     const int64_t nw = static_cast<int64_t>(gridDim.x) * kFlowWarps;
     for (int64_t x = static_cast<int64_t>(blockIdx.x) * kFlowWarps + warp; x < X; x += nw) {
         float* gx = gy + x * D;
@@ -258,28 +315,68 @@ __global__ void flow_layer_bwd_kernel(const LayerDev L, int64_t X, float* __rest
             g_o[x * O + J + j] = gt;
         }
         __syncwarp();
-        for (int h = lane; h < H; h += 32) {
-            float acc = 0.0f;
-            for (int c = 0; c < O; ++c) acc = fmaf(go[c], w3t[c * H + h], acc);
-            const float h2v = sv.h2[x * H + h];
-            const float v = acc * (1.0f - h2v * h2v);
-            gz2[h] = v;
-            g_z2[x * H + h] = v;
+        {
+            float acc[2][UPH], wv[UPH], hv[UPH];
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) { acc[0][u] = 0.f; acc[1][u] = 0.f; }
+            int c = 0;
+            for (; c + 1 < O; c += 2) {
+                const float a0 = go[c], a1 = go[c + 1];
+                ldu<UPH>(w3t + c * H + h0, wv);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[0][u] = fmaf(a0, wv[u], acc[0][u]);
+                ldu<UPH>(w3t + (c + 1) * H + h0, wv);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[1][u] = fmaf(a1, wv[u], acc[1][u]);
+            }
+            if (c < O) {
+                const float a0 = go[c];
+                ldu<UPH>(w3t + c * H + h0, wv);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[0][u] = fmaf(a0, wv[u], acc[0][u]);
+            }
+            const float* h2x = sv.h2 + x * H + h0;
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) hv[u] = h2x[u];
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) {
+                const float v = (acc[0][u] + acc[1][u]) * (1.0f - hv[u] * hv[u]);
+                gz2[h0 + u] = v;
+                g_z2[x * H + h0 + u] = v;
+            }
         }
         __syncwarp();
-        for (int h = lane; h < H; h += 32) {
-            float acc = 0.0f;
-            for (int m = 0; m < H; ++m) acc = fmaf(gz2[m], w2t[m * H + h], acc);
-            const float h1v = sv.h1[x * H + h];
-            const float v = acc * (1.0f - h1v * h1v);
-            gz1[h] = v;
-            g_z1[x * H + h] = v;
+        {
+            float acc[2][UPH], wv[UPH], hv[UPH];
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) { acc[0][u] = 0.f; acc[1][u] = 0.f; }
+            for (int m = 0; m < H; m += 2) {
+                const float a0 = gz2[m], a1 = gz2[m + 1];
+                ldu<UPH>(w2t + m * H + h0, wv);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[0][u] = fmaf(a0, wv[u], acc[0][u]);
+                ldu<UPH>(w2t + (m + 1) * H + h0, wv);
+#pragma unroll
+                for (int u = 0; u < UPH; ++u) acc[1][u] = fmaf(a1, wv[u], acc[1][u]);
+            }
+            const float* h1x = sv.h1 + x * H + h0;
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) hv[u] = h1x[u];
+#pragma unroll
+            for (int u = 0; u < UPH; ++u) {
+                const float v = (acc[0][u] + acc[1][u]) * (1.0f - hv[u] * hv[u]);
+                gz1[h0 + u] = v;
+                g_z1[x * H + h0 + u] = v;
+            }
         }
         __syncwarp();
         for (int i = lane; i < I; i += 32) {
-            float acc = 0.0f;
-            for (int k = 0; k < H; ++k) acc = fmaf(gz1[k], w1t[k * I + i], acc);
-            gx[L.idx_a[i]] += acc;
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int k = 0; k < H; k += 4) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) acc[u] = fmaf(gz1[k + u], w1t[(k + u) * IP + i], acc[u]);
+            }
+            gx[L.idx_a[i]] += (acc[0] + acc[1]) + (acc[2] + acc[3]);
         }
         __syncwarp();
     }
@@ -413,15 +510,19 @@ int status() { return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 
 int layer_smem_fwd(const pbr_flow_layer* l) {
     return static_cast<int>(sizeof(float)) *
-           (l->I * l->H + l->H * l->H + l->H * 2 * l->J + 2 * l->H + 2 * l->J + kFlowWarps * (l->I + 2 * l->H));
+           (l->I * l->H + l->H * l->H + l->H * 2 * l->J + 2 * l->H + align_up_(2 * l->J, 4) +
+            kFlowWarps * (align_up_(l->I, 4) + 2 * l->H));
 }
 int layer_smem_bwd(const pbr_flow_layer* l) {
     return static_cast<int>(sizeof(float)) *
-           (l->I * l->H + l->H * l->H + 2 * l->J * l->H + kFlowWarps * (2 * l->J + 2 * l->H));
+           (l->H * align_up_(l->I, 32) + l->H * l->H + 2 * l->J * l->H +
+            kFlowWarps * (align_up_(2 * l->J, 4) + 2 * l->H));
 }
 
+// hidden widths 32, 64, 128, 256: UPH = H / 32 units per lane
 bool layer_ok(const pbr_flow_layer* l) {
-    return l && l->D > 0 && l->I > 0 && l->J > 0 && l->H > 0 && l->I + l->J == l->D && l->idx_a &&
+    return l && l->D > 0 && l->I > 0 && l->J > 0 && (l->H == 32 || l->H == 64 || l->H == 128 || l->H == 256) &&
+           l->I + l->J == l->D && l->idx_a &&
            l->idx_b && l->W1 && l->b1 && l->W2 && l->b2 && l->W3 && l->b3;
 }
 
@@ -438,21 +539,24 @@ int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t ns
                      double* U, void* stream) {
     if (!q || !center || !inv_sigma || !rho_csch || !rho_tanh2 || !y || !U) return PBR_ERR_ARG;
     // slots beyond the cos/sin pairs (the alternating mode of an even ring) are not supported
-    if (X < 0 || N < 1 || P < 3 || nsel < 1 || nsel > 8 || nsel > 1 + 2 * ((P - 1) / 2)) return PBR_ERR_ARG;
+    if (X < 0 || N < 1 || P < 3 || P > 4096 || nsel < 1 || nsel > 8 || nsel > 1 + 2 * ((P - 1) / 2))
+        return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int threads = 128;
-    flow_prepare_kernel<<<grid_for(X * 32, threads), threads, 0, static_cast<cudaStream_t>(stream)>>>(
+    flow_prepare_kernel<<<grid_for(X * 32, threads), threads, nsel * P * sizeof(float),
+                          static_cast<cudaStream_t>(stream)>>>(
         q, X, N, P, nsel, center, inv_sigma, rho_csch, rho_tanh2, y, U);
     return status();
 }
 
 int pbr_flow_apply(const float* q, const float* y, const float* y_new, int64_t X, int32_t N, int32_t P,
                    int32_t nsel, const double* sigma, float* x, void* stream) {
-    if (!q || !y || !y_new || !sigma || !x || X < 0 || N < 1 || P < 3 || nsel < 1 || nsel > 8 ||
+    if (!q || !y || !y_new || !sigma || !x || X < 0 || N < 1 || P < 3 || P > 4096 || nsel < 1 || nsel > 8 ||
         nsel > 1 + 2 * ((P - 1) / 2))
         return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
-    flow_apply_kernel<<<grid_for(X * N * P, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+    flow_apply_kernel<<<grid_for(X * N * P, 256), 256, nsel * P * sizeof(float),
+                        static_cast<cudaStream_t>(stream)>>>(
         q, y, y_new, X, N, P, nsel, sigma, x);
     return status();
 }
@@ -468,14 +572,25 @@ int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64
     }
     const int bytes = layer_smem_fwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
-    if (bytes > 48 * 1024 &&
-        cudaFuncSetAttribute(flow_layer_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
-        return PBR_ERR_UNSUPPORTED;
-    const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
-    const int grid = static_cast<int>(blocks < sm_count() * 2 ? blocks : sm_count() * 2);
-    flow_layer_fwd_kernel<<<grid, kFlowWarps * 32, bytes, static_cast<cudaStream_t>(stream)>>>(
-        to_dev(layer), direction, X, y, logdet, sv);
-    return status();
+    auto go = [&](auto kern) -> int {
+        if (bytes > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+            return PBR_ERR_UNSUPPORTED;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kFlowWarps * 32, bytes) != cudaSuccess || occ < 1)
+            return PBR_ERR_UNSUPPORTED;
+        const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
+        const int cap = sm_count() * occ;
+        kern<<<static_cast<int>(blocks < cap ? blocks : cap), kFlowWarps * 32, bytes,
+               static_cast<cudaStream_t>(stream)>>>(to_dev(layer), direction, X, y, logdet, sv);
+        return status();
+    };
+    switch (layer->H) {
+        case 32: return go(flow_layer_fwd_kernel<1>);
+        case 64: return go(flow_layer_fwd_kernel<2>);
+        case 128: return go(flow_layer_fwd_kernel<4>);
+        default: return go(flow_layer_fwd_kernel<8>);
+    }
 }
 
 int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, const float* rt,
@@ -485,15 +600,26 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
     if (X == 0) return PBR_OK;
     const int bytes = layer_smem_bwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
-    if (bytes > 48 * 1024 &&
-        cudaFuncSetAttribute(flow_layer_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
-        return PBR_ERR_UNSUPPORTED;
     const SaveDev sv{save->ya, save->h1, save->h2, save->s, save->yb};
-    const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
-    const int grid = static_cast<int>(blocks < sm_count() * 2 ? blocks : sm_count() * 2);
-    flow_layer_bwd_kernel<<<grid, kFlowWarps * 32, bytes, static_cast<cudaStream_t>(stream)>>>(
-        to_dev(layer), X, gy, rt, sv, g_o, g_z2, g_z1);
-    return status();
+    auto go = [&](auto kern) -> int {
+        if (bytes > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+            return PBR_ERR_UNSUPPORTED;
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kFlowWarps * 32, bytes) != cudaSuccess || occ < 1)
+            return PBR_ERR_UNSUPPORTED;
+        const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
+        const int cap = sm_count() * occ;
+        kern<<<static_cast<int>(blocks < cap ? blocks : cap), kFlowWarps * 32, bytes,
+               static_cast<cudaStream_t>(stream)>>>(to_dev(layer), X, gy, rt, sv, g_o, g_z2, g_z1);
+        return status();
+    };
+    switch (layer->H) {
+        case 32: return go(flow_layer_bwd_kernel<1>);
+        case 64: return go(flow_layer_bwd_kernel<2>);
+        case 128: return go(flow_layer_bwd_kernel<4>);
+        default: return go(flow_layer_bwd_kernel<8>);
+    }
 }
 
 int64_t pbr_gemm_tn_scratch(int64_t X, int32_t M, int32_t N) {

@@ -146,6 +146,78 @@ __global__ void final_merge(const double* scratch, int nblocks, double* out) {
     }
 }
 
+// ---- segmented variants: one independent reduction per model of a batched launch -----------
+constexpr int kSegChunks = 32;
+
+__global__ void terms_partial_seg(const double* rho, const double* g, const double* gp, const double* gm,
+                                  const int64_t* seg, const double* dbeta, double* scratch) {
+    const int m = blockIdx.y, c = blockIdx.x;
+    const int64_t s0 = seg[m], s1 = seg[m + 1];
+    const int64_t len = s1 - s0, chunk = (len + kSegChunks - 1) / kSegChunks;
+    const int64_t c0 = s0 + c * chunk, c1 = min(s1, c0 + chunk);
+    Moments mo[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+        double r, a, b;
+        terms(rho, g, gp, gm, i, dbeta[m], r, a, b);
+        push(mo[0], r);
+        push(mo[1], a);
+        push(mo[2], b);
+    }
+    block_merge<3>(mo);
+    if (threadIdx.x == 0)
+        for (int v = 0; v < 3; ++v) {
+            double* o = scratch + ((static_cast<int64_t>(m) * kSegChunks + c) * 3 + v) * 3;
+            o[0] = mo[v].n; o[1] = mo[v].mean; o[2] = mo[v].m2;
+        }
+}
+
+__global__ void jackknife_partial_seg(const double* rho, const double* g, const double* gp, const double* gm,
+                                      const int64_t* seg, const double* dbeta, const double* kT2,
+                                      const double* moments, double* scratch) {
+    const int m = blockIdx.y, c = blockIdx.x;
+    const int64_t s0 = seg[m], s1 = seg[m + 1];
+    const int64_t len = s1 - s0, chunk = (len + kSegChunks - 1) / kSegChunks;
+    const int64_t c0 = s0 + c * chunk, c1 = min(s1, c0 + chunk);
+    const double* mm = moments + m * 7;
+    const double Sr = mm[0] * mm[1], S1 = mm[0] * mm[3], S2 = mm[0] * mm[5];
+    const double E0 = -S1 / Sr;
+    Moments mo[2] = {{0, 0, 0}, {0, 0, 0}};
+    for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
+        double r, a, b;
+        terms(rho, g, gp, gm, i, dbeta[m], r, a, b);
+        const double den = Sr * (Sr - r);
+        const double dE = (Sr * a - S1 * r) / den;
+        const double dC = (-(Sr * b - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2[m];
+        push(mo[0], dE);
+        push(mo[1], dC);
+    }
+    block_merge<2>(mo);
+    if (threadIdx.x == 0)
+        for (int v = 0; v < 2; ++v) {
+            double* o = scratch + ((static_cast<int64_t>(m) * kSegChunks + c) * 2 + v) * 3;
+            o[0] = mo[v].n; o[1] = mo[v].mean; o[2] = mo[v].m2;
+        }
+}
+
+template <int V>
+__global__ void final_merge_seg(const double* scratch, double* out) {
+    const int m = blockIdx.x;
+    if (threadIdx.x != 0) return;
+    Moments acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = Moments{0, 0, 0};
+    for (int c = 0; c < kSegChunks; ++c)
+#pragma unroll
+        for (int v = 0; v < V; ++v) {
+            const double* s = scratch + ((static_cast<int64_t>(m) * kSegChunks + c) * V + v) * 3;
+            acc[v] = merge(acc[v], Moments{s[0], s[1], s[2]});
+        }
+    double* o = out + m * (1 + 2 * V);
+    o[0] = acc[0].n;
+#pragma unroll
+    for (int v = 0; v < V; ++v) { o[1 + 2 * v] = acc[v].mean; o[2 + 2 * v] = acc[v].m2; }
+}
+
 int nblocks_for(int64_t X) {
     int64_t nb = (X + kPerBlock - 1) / kPerBlock;
     if (nb < 1) nb = 1;
@@ -158,6 +230,32 @@ int nblocks_for(int64_t X) {
 extern "C" {
 
 int64_t pbr_reduce_blocks(int64_t X) { return nblocks_for(X); }
+
+int64_t pbr_reduce_segments_scratch(int32_t M) { return static_cast<int64_t>(M) * kSegChunks * 9; }
+
+int pbr_reduce_terms_segments(const double* s_rho, const double* s_g, const double* s_gp, const double* s_gm,
+                              const int64_t* seg, int32_t M, const double* delta_beta, double* scratch,
+                              double* moments, void* stream) {
+    if (!s_rho || !s_g || !seg || !delta_beta || !scratch || !moments || M < 1 || M > 65535) return PBR_ERR_ARG;
+    if ((s_gp == nullptr) != (s_gm == nullptr)) return PBR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    terms_partial_seg<<<dim3(kSegChunks, M), kRedThreads, 0, st>>>(s_rho, s_g, s_gp, s_gm, seg, delta_beta, scratch);
+    final_merge_seg<3><<<M, 32, 0, st>>>(scratch, moments);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+int pbr_reduce_jackknife_segments(const double* s_rho, const double* s_g, const double* s_gp, const double* s_gm,
+                                  const int64_t* seg, int32_t M, const double* delta_beta, const double* kB_T2,
+                                  const double* moments, double* scratch, double* out, void* stream) {
+    if (!s_rho || !s_g || !s_gp || !s_gm || !seg || !delta_beta || !kB_T2 || !moments || !scratch || !out ||
+        M < 1 || M > 65535)
+        return PBR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    jackknife_partial_seg<<<dim3(kSegChunks, M), kRedThreads, 0, st>>>(s_rho, s_g, s_gp, s_gm, seg, delta_beta,
+                                                                       kB_T2, moments, scratch);
+    final_merge_seg<2><<<M, 32, 0, st>>>(scratch, out);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
 
 int pbr_reduce_terms(const double* s_rho, const double* s_g, const double* s_gp,
                      const double* s_gm, int64_t X, double delta_beta, double* scratch,

@@ -48,6 +48,8 @@ __host__ __device__ inline int record_len(int A, int K) { return align_up(A * A 
 
 struct TeamPlan {
     int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
+    __host__ __device__ TeamPlan() : c(0), e(0), qq(0), rc(0), rec(0), src(0), q(0), qlo(0), beads(0),
+                                     lsums(0), total_bytes(0) {}
     __host__ __device__ TeamPlan(int A, int K, int qm, int esz, int N, int P, int S, int G, int qstride,
                                  int rl) {
         const int A2P = align_up(npair(A), 4);
@@ -67,34 +69,19 @@ struct TeamPlan {
     }
 };
 
+// Copy one model's tables into the CTA's shared memory (layout TeamPlan).
 template <int A, int K, int QM, typename T>
-__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kernel(const TeamArgs args) {
+__device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
     constexpr int KP = (K + 1 + 3) / 4 * 4;
     constexpr int AP = (A + 3) / 4 * 4;
     constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
-    constexpr int TA = (A <= 1) ? 1 : (A <= 2) ? 2 : (A <= 4) ? 4 : 8;
-    constexpr int OFF_O = A * A, OFF_L = A * A + (K + 1) * A, OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
-    constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
     constexpr int NT = kTeamThreads;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sm = reinterpret_cast<T*>(smem_raw);
-
-    const pbr_model& m = args.m;
-    const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
-    const int S = args.S, G = args.G, C = args.C, RL = args.rl;
-    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, G, args.qstride, RL);
+    const int N = m.N, nfill = m.n_fill_rho;
+    const int tid = threadIdx.x;
     T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
     T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec;
-    int* s_src = reinterpret_cast<int*>(sm + plan.src);
-    T* s_q = sm + plan.q;
-    T* s_ql = kLo ? sm + plan.qlo : nullptr;
-    T* s_beads = sm + plan.beads;
-    double* s_lsum = reinterpret_cast<double*>(sm + plan.lsums);
-    const int tid = threadIdx.x;
-
-    // ---- model tables -> shared memory (once per CTA; the grid is persistent) -----------------
     {
         const T* g_cs = static_cast<const T*>(m.vib_cs);  const T* g_th = static_cast<const T*>(m.vib_th);
         const T* g_c = static_cast<const T*>(m.vib_c);    const T* g_d = static_cast<const T*>(m.vib_d);
@@ -123,7 +110,34 @@ __global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kern
             s_rec[i] = v;
         }
     }
-    __syncthreads();
+}
+
+// One tile of S samples starting at global sample `base` (phases A, B1, B2, C, D); ends with a
+// block barrier, so the caller may reload the tables afterwards.
+template <int A, int K, int QM, typename T>
+__device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int64_t base) {
+    constexpr int A2 = npair(A);
+    constexpr int A2P = (A2 + 3) / 4 * 4;
+    constexpr int KP = (K + 1 + 3) / 4 * 4;
+    constexpr int AP = (A + 3) / 4 * 4;
+    constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
+    constexpr int TA = (A <= 1) ? 1 : (A <= 2) ? 2 : (A <= 4) ? 4 : 8;
+    constexpr int OFF_O = A * A, OFF_L = A * A + (K + 1) * A, OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
+    constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
+    constexpr int NT = kTeamThreads;
+
+    const pbr_model& m = args.m;
+    const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
+    const int S = args.S, G = args.G, C = args.C, RL = args.rl;
+    T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
+    T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec;
+    int* s_src = reinterpret_cast<int*>(sm + plan.src);
+    T* s_q = sm + plan.q;
+    T* s_ql = kLo ? sm + plan.qlo : nullptr;
+    T* s_beads = sm + plan.beads;
+    double* s_lsum = reinterpret_cast<double*>(sm + plan.lsums);
+    const int tid = threadIdx.x;
+
 
     const T tau_l2 = T(m.tau * 1.4426950408889634);   // tau * log2(e)
     const int NP = N * P;
@@ -135,8 +149,7 @@ __global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kern
     const unsigned tmask = (TA == 32) ? 0xffffffffu : (((1u << TA) - 1u) << (lane & ~(TA - 1)));
     const int CL = (K + 1) * A * A + 4;                    // combine slot length
 
-    for (int64_t base = static_cast<int64_t>(blockIdx.x) * S; base < args.X;
-         base += static_cast<int64_t>(gridDim.x) * S) {
+    {
         const int nvalid = static_cast<int>(min(static_cast<int64_t>(S), args.X - base));
 
         // ================================ phase A ==============================================
@@ -517,7 +530,60 @@ __global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kern
     }
 }
 
+template <int A, int K, int QM, typename T>
+__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kernel(const TeamArgs args) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sm = reinterpret_cast<T*>(smem_raw);
+    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
+                        args.qstride, args.rl);
+    team_load_tables<A, K, QM, T>(args.m, sm, plan);
+    __syncthreads();
+    for (int64_t base = static_cast<int64_t>(blockIdx.x) * args.S; base < args.X;
+         base += static_cast<int64_t>(gridDim.x) * args.S)
+        team_tile<A, K, QM, T>(args, sm, plan, base);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Many independent models in one persistent launch (all with the same surface count A and series
+// order K): the work is the concatenation of every model's tiles; CTAs take tiles round-robin,
+// find the owning model by binary search over the tile prefix, and reload that model's tables
+// into shared memory when it changes.  Each model keeps its own sizes (N, P), temperature, tile
+// shape (S, G, C), seed, counter offset and outputs.
+// ---------------------------------------------------------------------------------------------
+struct TeamBatchItem {
+    TeamArgs a;
+    int64_t tile_begin;       // first tile of this model in the launch
+};
+
+template <int A, int K>
+__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1))
+pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int64_t total_tiles) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sm = reinterpret_cast<float*>(smem_raw);
+    int cur = -1;
+    TeamPlan plan;
+    for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+        int lo = 0, hi = n_items - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+        }
+        const TeamArgs& a = items[lo].a;
+        if (lo != cur) {
+            plan = TeamPlan(A, K, kSample, 4, a.m.N, a.m.P, a.S, a.G, a.qstride, a.rl);
+            team_load_tables<A, K, kSample, float>(a.m, sm, plan);
+            __syncthreads();
+            cur = lo;
+        }
+        team_tile<A, K, kSample, float>(a, sm, plan, (t - items[lo].tile_begin) * a.S);
+    }
+}
+
 template <int A>
 int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStream_t stream);
+
+template <int A>
+int launch_team_batch(int K, const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
+                      int grid_cap, cudaStream_t stream);
 
 }  // namespace pbr

@@ -53,4 +53,30 @@ int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStrea
     return launch_team_one<A, 4, kQ64, double>(args, stream);
 }
 
+template <int A, int K>
+static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
+                                 int grid_cap, cudaStream_t stream) {
+    auto kern = pimc_team_batch_kernel<A, K>;
+    if (smem_bytes > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) != cudaSuccess)
+        return PBR_ERR_UNSUPPORTED;
+    int dev = 0, sms = 0, occ = 0;
+    PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
+    PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTeamThreads, smem_bytes));
+    if (occ < 1) return PBR_ERR_UNSUPPORTED;
+    int64_t grid = std::min<int64_t>(total_tiles, static_cast<int64_t>(occ) * sms);
+    if (grid_cap > 0) grid = std::min<int64_t>(grid, grid_cap);
+    if (grid <= 0) return PBR_OK;
+    kern<<<static_cast<int>(grid), kTeamThreads, smem_bytes, stream>>>(items, n_items, total_tiles);
+    return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+template <int A>
+int launch_team_batch(int K, const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
+                      int grid_cap, cudaStream_t stream) {
+    if (K == 0) return launch_team_batch_one<A, 0>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
+    return launch_team_batch_one<A, 4>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
+}
+
 }  // namespace pbr

@@ -199,12 +199,11 @@ class FlowProposal:
         hist = []
         for ep in range(epochs):
             perm = torch.randperm(X, generator=gen).to(self.dev)
-            tot = 0.0
+            tot = torch.zeros((), dtype=torch.float64, device=self.dev)
             for b0 in range(0, X - batch + 1, batch):
                 idx = perm[b0:b0 + batch]
-                loss = self.train_step(y[idx].contiguous(), r[idx].contiguous(), lr)
-                tot += loss
-            hist.append(tot / max(1, X // batch))
+                tot += self.train_step(y[idx].contiguous(), r[idx].contiguous(), lr)
+            hist.append(float(tot.item()) / max(1, X // batch))
             if log:
                 log(f"epoch {ep}: mean batch loss {hist[-1]:.6f}")
         return hist
@@ -267,9 +266,10 @@ class FlowProposal:
         gsum = torch.empty(self.A, dtype=torch.float32, device=self.dev)
         _native.check(lib.pbr_colsum(p(rgam), B, self.A, p(gsum), sh), "nu gradient")
         g_nu = -(gsum - torch.exp(lp) * rt.sum())
-        return float(lterm.sum().item()), grads, g_nu
+        return lterm.sum(), grads, g_nu
 
     def train_step(self, y, r, lr):
+        """One Adam step; returns the batch loss as a device scalar (no host synchronisation)."""
         loss, grads, g_nu = self.gradients(y, r)
         self._adam_step(grads, g_nu, lr)
         return loss

@@ -62,6 +62,26 @@ def write_model_pair(FS, A, N, seed, **kw):
     return model
 
 
+def batch_models(count=256, seed=3, A_range=(2, 8), N_range=(3, 20), P_range=(8, 256), T_range=(100.0, 500.0),
+                 rel_delta_beta=1e-4):
+    """Seeded independent models of uneven sizes for the batched configuration: A ~ U{2..8},
+    N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, each with the coupled-model recipe above and
+    rho its diagonal.  Returns PreparedModels (beta +- rel_delta_beta * beta series)."""
+    from .constants import beta as beta_of
+    from .plan import PreparedModels
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        A = int(rng.integers(A_range[0], A_range[1] + 1))
+        N = int(rng.integers(N_range[0], N_range[1] + 1))
+        P = int(rng.integers(P_range[0], P_range[1] + 1))
+        T = float(rng.uniform(*T_range))
+        m = make_coupled_model(A, N, seed * 100003 + i)
+        b = beta_of(T)
+        out.append(PreparedModels(m, diagonal_of(m), P, beta=b, delta_beta=rel_delta_beta * b))
+    return out
+
+
 #: benchmark configurations (sizes of the reference's headline runs)
 CONFIGS = {
     1: dict(A=2, N=2, P=12, T=300.0, X=10_000, B=1_000),

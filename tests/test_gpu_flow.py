@@ -53,7 +53,8 @@ def test_prepare_matches_numpy(tmp_path):
     lam_q = (2 / np.tanh(tau * w))[None, :] * (x ** 2).sum(axis=2) \
         - (1 / np.sinh(tau * w))[None, :] * 2 * (x * np.roll(x, -1, axis=2)).sum(axis=2)
     Uref = lam_q.sum(axis=1) - (yref ** 2).sum(axis=(1, 2))
-    assert np.allclose(U.cpu().numpy(), Uref, rtol=1e-8, atol=1e-8)
+    # FP32 terms per lane, FP64 across lanes and modes: ~1e-7 relative (a weight moves by e^(dU/2))
+    assert np.allclose(U.cpu().numpy(), Uref, rtol=1e-6, atol=1e-6)
 
 
 def test_layers_match_oracle(tmp_path):
@@ -82,7 +83,7 @@ def test_gradients_match_oracle(tmp_path):
     ref_loss, ref_grads, ref_gnu = fo.loss_and_grads(fl.params_host(), fl.nu.double().cpu().numpy(),
                                                      y.double().cpu().numpy(), r.cpu().numpy(),
                                                      fl.t_mu.double().cpu().numpy(), fl.log_w)
-    assert math.isclose(loss, ref_loss, rel_tol=1e-4, abs_tol=1e-5)
+    assert math.isclose(float(loss), ref_loss, rel_tol=1e-4, abs_tol=1e-5)
     for l in range(4):
         for k, v in grads[l].items():
             ref = ref_grads[l][k]

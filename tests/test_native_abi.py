@@ -9,7 +9,7 @@ from conftest import REPO
 
 def declared_symbols():
     text = open(os.path.join(REPO, "include", "pibronic_gb300.h")).read()
-    return sorted(set(re.findall(r"^(?:int|int64_t|const char\*)\s+(pbr_\w+)\(", text, re.M)))
+    return sorted(set(re.findall(r"^(?:int|int32_t|int64_t|const char\*)\s+(pbr_\w+)\(", text, re.M)))
 
 
 def test_header_declares_the_binding_list():
