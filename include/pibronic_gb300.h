@@ -119,6 +119,21 @@ int pbr_sample_eval(const pbr_model* model, uint64_t seed, uint64_t offset, int6
                     const pbr_outputs* out, void* stream);
 
 /*
+ * The same block evaluation with the quadratic coupling contraction on the tensor cores, for
+ * large N (precision 32 only): per chunk of samples the sampler writes q (into out->q_out when
+ * given, else into scratch), the tcgen05 contraction (TF32, hi/lo split, three MMAs per K step)
+ * writes the quadratic part of V for every (sample, bead) row, and the row-team kernel evaluates
+ * the chunk from q and that V.  Draws the same samples as pbr_sample_eval for the same seed and
+ * offset.  scratch (256-byte aligned, scratch_bytes long) bounds the chunk:
+ * pbr_sample_eval_tc_scratch(model, chunk) is the size for a chunk of that many samples; a
+ * scratch too small for one sample gives PBR_ERR_CAPACITY.  Replaces the same reference stages
+ * as pbr_sample_eval (the quadratic term is pimc.py:1147).
+ */
+int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk);
+int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X,
+                       const pbr_outputs* out, void* scratch, int64_t scratch_bytes, void* stream);
+
+/*
  * Many independent models in one launch per surface count (the batched configuration): every
  * model keeps its own sizes, temperature, seed, counter offset and outputs.  pbr_batch_pack fills
  * a host blob of pbr_batch_blob_bytes(n) bytes (tile shapes per model within smem_budget bytes of
@@ -349,6 +364,23 @@ int pbr_adam(float* param, const float* grad, float* m, float* v, int64_t n, flo
  */
 int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, int32_t N, int32_t K,
                 int32_t* status, void* stream);
+
+/*
+ * The quadratic coupling contraction alone (the middle stage of pbr_sample_eval_tc), for tests and
+ * custom pipelines.  pbr_tc_quadratic_dims gives the padded K extent n2p (pairs d >= e of modes,
+ * a multiple of 32) and column count a2p (pairs b >= c of surfaces, a multiple of 16).
+ * pbr_tc_pack_quadratic turns vib_qq ([N(N+1)/2][A(A+1)/2], FP32 or FP64 as precision says) into
+ * the TF32 hi / lo operands b_hi, b_lo [a2p][n2p] (16-byte aligned).  pbr_tc_quadratic writes
+ * vq [X * P][a2p] (FP32; row sample * P + bead, column pair_index(b, c)) =
+ * sum_{d >= e} q_d q_e vib_qq[pair_index(d, e)][pair_index(b, c)] from q [X][N][P] (FP32).
+ * Waits are bounded as in pbr_tc_gemm.  Replaces pimc.py:1147 (the quadratic einsum of
+ * build_denominator / build_numerator's V).
+ */
+int pbr_tc_quadratic_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
+int pbr_tc_pack_quadratic(const void* vib_qq, int32_t precision, int32_t N, int32_t A, float* b_hi,
+                          float* b_lo, void* stream);
+int pbr_tc_quadratic(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const float* b_hi,
+                     const float* b_lo, float* vq, int32_t* status, void* stream);
 
 /* Library version string and the SM architecture it was built for. */
 const char* pbr_version(void);

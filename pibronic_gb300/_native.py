@@ -33,7 +33,8 @@ EXPORTED = (
     "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
     "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
     "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
-    "pbr_tc_gemm", "pbr_version",
+    "pbr_tc_gemm", "pbr_tc_quadratic_dims", "pbr_tc_pack_quadratic", "pbr_tc_quadratic",
+    "pbr_sample_eval_tc_scratch", "pbr_sample_eval_tc", "pbr_version",
 )
 
 
@@ -117,6 +118,11 @@ def _declare(lib):
         "pbr_reduce_jackknife_segments": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]),
         "pbr_reduce_segments_scratch": (i64, [i32]),
         "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
+        "pbr_tc_quadratic_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
+        "pbr_tc_pack_quadratic": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
+        "pbr_tc_quadratic": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, vp]),
+        "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),
+        "pbr_sample_eval_tc": (C.c_int, [C.POINTER(PbrModel), u64, u64, i64, C.POINTER(PbrOutputs), vp, i64, vp]),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

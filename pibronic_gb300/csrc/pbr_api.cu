@@ -8,6 +8,11 @@ namespace pbr {
 template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
 template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
 template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, cudaStream_t);
+int tc_quadratic_cols(int A);
+int tc_quadratic_kdim(int N);
+int tc_quadratic_launch(const float*, int64_t, int, int, int, const float*, const float*, int, float*, int32_t*,
+                        cudaStream_t);
+int tc_pack_launch(const void*, int, int, int, float*, float*, cudaStream_t);
 }
 
 namespace {
@@ -67,11 +72,14 @@ int team_smem(const pbr::TeamArgs& a, int qmode) {
 }
 
 int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
-             uint64_t offset, const pbr_outputs* out, cudaStream_t st) {
+             uint64_t offset, const pbr_outputs* out, cudaStream_t st, const float* vq = nullptr,
+             int vq_ld = 0) {
     using namespace pbr;
     TeamArgs a;
     const int rc = make_team_args(m, qmode, q_in, X, seed, offset, out, kMaxSmem, &a);
     if (rc != PBR_OK) return rc;
+    a.vq = vq;
+    a.vq_ld = vq_ld;
     switch (m.A) {
         case 1: return launch_team<1>(m.K, qmode, m.precision, a, st);
         case 2: return launch_team<2>(m.K, qmode, m.precision, a, st);
@@ -85,14 +93,10 @@ int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_
     }
 }
 
-int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, uint64_t seed,
-              uint64_t offset, const pbr_outputs* out, void* stream) {
+int check_model(const pbr_model& m, int qmode, const void* q_in, const pbr_outputs* out) {
     using namespace pbr;
-    if (!model || !out || X < 0) return PBR_ERR_ARG;
-    if (X == 0) return PBR_OK;
-    const pbr_model& m = *model;
     if (m.A < 1 || m.A > PBR_MAX_A) return PBR_ERR_UNSUPPORTED;
-    if (m.variant < 0 || m.variant > 2) return PBR_ERR_ARG;
+    if (m.variant < 0 || m.variant > 3) return PBR_ERR_ARG;
     if (m.A_rho < m.A || m.A_rho > PBR_MAX_A_RHO) return PBR_ERR_ARG;
     if (m.n_fill_rho != m.A) return PBR_ERR_ARG;
     if (m.N < 1 || m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P) return PBR_ERR_ARG;
@@ -105,7 +109,18 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
         return PBR_ERR_ARG;
     if (qmode == kSample && (!m.ring_chol || !m.src_cdf)) return PBR_ERR_ARG;
     if (qmode != kSample && !q_in) return PBR_ERR_ARG;
-    const bool team = m.variant == 2 || (m.variant == 0 && m.A > 4);
+    return PBR_OK;
+}
+
+int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, uint64_t seed,
+              uint64_t offset, const pbr_outputs* out, void* stream) {
+    using namespace pbr;
+    if (!model || !out || X < 0) return PBR_ERR_ARG;
+    if (X == 0) return PBR_OK;
+    const pbr_model& m = *model;
+    const int chk = check_model(m, qmode, q_in, out);
+    if (chk != PBR_OK) return chk;
+    const bool team = m.variant >= 2 || (m.variant == 0 && m.A > 4);
     if (team) return run_team(m, qmode, q_in, X, seed, offset, out, static_cast<cudaStream_t>(stream));
     if (m.A > 4) return PBR_ERR_UNSUPPORTED;
 
@@ -311,5 +326,87 @@ int32_t pbr_batch_groups(const void* host_blob) {
 }
 
 const char* pbr_version(void) { return "pibronic_gb300 0.1 sm_103a"; }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Tensor-core form: per chunk of samples, (1) the sampler writes q, (2) the tcgen05 contraction
+// writes the quadratic coupling part of V for every (sample, bead) row, (3) the row-team kernel
+// evaluates the chunk from q and that V.  The chunk is sized by the caller's scratch; about
+// 64 MB of q and V per chunk keeps both resident in L2 between the three launches.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kScratchAlign = 256;
+
+int64_t align_bytes(int64_t n) { return (n + kScratchAlign - 1) / kScratchAlign * kScratchAlign; }
+
+int64_t tc_fixed_bytes(const pbr_model& m) {
+    const int64_t b = static_cast<int64_t>(pbr::tc_quadratic_cols(m.A)) * pbr::tc_quadratic_kdim(m.N) * 4;
+    return 2 * align_bytes(b) + kScratchAlign;
+}
+
+int64_t tc_sample_bytes(const pbr_model& m) {
+    return static_cast<int64_t>(m.N) * m.P * 4 + static_cast<int64_t>(m.P) * pbr::tc_quadratic_cols(m.A) * 4;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk) {
+    if (!model || chunk < 1 || model->A < 1 || model->A > PBR_MAX_A || model->N < 1 || model->N > PBR_MAX_N ||
+        model->P < 3 || model->P > PBR_MAX_P)
+        return -1;
+    return tc_fixed_bytes(*model) + 2 * kScratchAlign + chunk * tc_sample_bytes(*model);
+}
+
+int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X, const pbr_outputs* out,
+                       void* scratch, int64_t scratch_bytes, void* stream) {
+    using namespace pbr;
+    if (!model || !out || X < 0 || !scratch) return PBR_ERR_ARG;
+    if (X == 0) return PBR_OK;
+    const pbr_model& m = *model;
+    const int chk = check_model(m, kSample, nullptr, out);
+    if (chk != PBR_OK) return chk;
+    if (m.precision != 32) return PBR_ERR_UNSUPPORTED;        // TF32 split: the FP32 form only
+    if (reinterpret_cast<uintptr_t>(scratch) % kScratchAlign) return PBR_ERR_ARG;
+    const int64_t per = tc_sample_bytes(m);
+    const int64_t chunk = (scratch_bytes - tc_fixed_bytes(m) - 2 * kScratchAlign) / per;
+    if (chunk < 1) return PBR_ERR_CAPACITY;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int A2P = tc_quadratic_cols(m.A), N2P = tc_quadratic_kdim(m.N);
+    unsigned char* base = static_cast<unsigned char*>(scratch);
+    const int64_t bbytes = align_bytes(static_cast<int64_t>(A2P) * N2P * 4);
+    float* b_hi = reinterpret_cast<float*>(base);
+    float* b_lo = reinterpret_cast<float*>(base + bbytes);
+    float* qbuf = reinterpret_cast<float*>(base + tc_fixed_bytes(m));
+    float* vq = reinterpret_cast<float*>(base + tc_fixed_bytes(m) +
+                                         align_bytes(chunk * static_cast<int64_t>(m.N) * m.P * 4));
+    int rc = tc_pack_launch(m.vib_qq, m.precision, m.N, m.A, b_hi, b_lo, st);
+    if (rc != PBR_OK) return rc;
+    const int K1 = m.K + 1;
+    for (int64_t c0 = 0; c0 < X; c0 += chunk) {
+        const int64_t n = std::min(chunk, X - c0);
+        float* qc = out->q_out ? out->q_out + c0 * static_cast<int64_t>(m.N) * m.P : qbuf;
+        rc = pbr_sample_q(model, seed, offset + static_cast<uint64_t>(c0), n, qc,
+                          out->src_out ? out->src_out + c0 : nullptr, stream);
+        if (rc != PBR_OK) return rc;
+        rc = tc_quadratic_launch(qc, n, m.N, m.P, A2P, b_hi, b_lo, N2P, vq, out->status, st);
+        if (rc != PBR_OK) return rc;
+        pbr_outputs oc = *out;
+        oc.s_rho = out->s_rho + c0;
+        oc.s_g = out->s_g + c0;
+        oc.s_gp = out->s_gp ? out->s_gp + c0 : nullptr;
+        oc.s_gm = out->s_gm ? out->s_gm + c0 : nullptr;
+        oc.g_coef = out->g_coef ? out->g_coef + c0 * K1 : nullptr;
+        oc.log_scale = out->log_scale ? out->log_scale + c0 : nullptr;
+        oc.q_out = nullptr;
+        oc.src_out = nullptr;
+        rc = run_team(m, kQ32V, qc, n, 0, 0, &oc, st, vq, A2P);
+        if (rc != PBR_OK) return rc;
+    }
+    return PBR_OK;
+}
 
 }  // extern "C"

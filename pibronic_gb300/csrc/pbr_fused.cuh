@@ -26,7 +26,9 @@ namespace pbr {
 
 constexpr int kThreads = 128;
 constexpr int kMaxChunk = 8;       // target beads per thread (chunk length) of the ring product
-enum QMode : int { kSample = 0, kQ64 = 1, kQ32 = 2 };
+// kQ32V: q from the caller (FP32) and the quadratic coupling part of V(q) precomputed per
+// (sample, bead) row by the tensor-core contraction (row-team form only)
+enum QMode : int { kSample = 0, kQ64 = 1, kQ32 = 2, kQ32V = 3 };
 
 struct FusedArgs {
     pbr_model m;

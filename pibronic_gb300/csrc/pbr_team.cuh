@@ -35,6 +35,8 @@ struct TeamArgs {
     int rs;         // q row stride (skewed layout, qidx)
     int qstride;    // q elements per sample
     int rl;         // bead record length
+    const float* vq;  // kQ32V: quadratic part of V, row (sample * P + bead), A(A+1)/2 used columns
+    int vq_ld;        // kQ32V: floats per row of vq
 };
 
 __host__ __device__ inline int pow2_ceil(int x) {
@@ -55,7 +57,7 @@ struct TeamPlan {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
+        c = take((K + 1) * A); e = take(A2P); qq = take(qm == kQ32V ? 0 : npair(N) * A2P); rc = take(A);
         rec = take(N * rec_len(A, K));
         src = take(S);                                             // ints stored in the slot
         q = take(S * qstride);
@@ -91,7 +93,7 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
         const T* g_rc = static_cast<const T*>(m.rho_c);   const T* g_rd = static_cast<const T*>(m.rho_d);
         for (int i = tid; i < (K + 1) * A; i += NT) s_c[i] = g_c[i];
         for (int i = tid; i < A2P; i += NT) s_e[i] = (i < A2) ? g_e[i] : T(0);
-        const int N2 = npair(N);
+        const int N2 = (QM == kQ32V) ? 0 : npair(N);
         for (int i = tid; i < N2 * A2P; i += NT) {
             const int row = i / A2P, col = i - row * A2P;
             s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
@@ -275,7 +277,17 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     for (int k = 0; k <= K; ++k) rec_out[OFF_O + k * A + a] = e0 * ek[k];
                 }
             }
-            {
+            if (QM == kQ32V) {
+                const float* vr = args.vq + ((base + s) * static_cast<int64_t>(P) + p) * args.vq_ld;
+#pragma unroll
+                for (int pr = 0; pr < A2; pr += 4) {
+                    const float4 w = *reinterpret_cast<const float4*>(vr + pr);
+                    v[pr] += T(w.x);
+                    if (pr + 1 < A2) v[pr + 1] += T(w.y);
+                    if (pr + 2 < A2) v[pr + 2] += T(w.z);
+                    if (pr + 3 < A2) v[pr + 3] += T(w.w);
+                }
+            } else {
                 int row = 0;
                 for (int d = 0; d < N; ++d) {
                     const T qd = qs[ip + d * rs];

@@ -38,13 +38,15 @@ int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStrea
         if (K == 0) {
             if (qmode == kSample) return launch_team_one<A, 0, kSample, float>(args, stream);
             if (qmode == kQ64) return launch_team_one<A, 0, kQ64, float>(args, stream);
+            if (qmode == kQ32V) return launch_team_one<A, 0, kQ32V, float>(args, stream);
             return launch_team_one<A, 0, kQ32, float>(args, stream);
         }
         if (qmode == kSample) return launch_team_one<A, 4, kSample, float>(args, stream);
         if (qmode == kQ64) return launch_team_one<A, 4, kQ64, float>(args, stream);
+        if (qmode == kQ32V) return launch_team_one<A, 4, kQ32V, float>(args, stream);
         return launch_team_one<A, 4, kQ32, float>(args, stream);
     }
-    if (qmode == kQ32) return PBR_ERR_UNSUPPORTED;
+    if (qmode == kQ32 || qmode == kQ32V) return PBR_ERR_UNSUPPORTED;
     if (K == 0) {
         if (qmode == kSample) return launch_team_one<A, 0, kSample, double>(args, stream);
         return launch_team_one<A, 0, kQ64, double>(args, stream);

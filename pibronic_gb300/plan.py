@@ -235,9 +235,16 @@ class DevicePlan:
     FIELDS = ("vib_cs", "vib_th", "vib_c", "vib_d", "vib_e", "vib_l", "vib_qq", "rho_cs", "rho_th",
               "rho_c", "rho_d", "ring_chol", "src_cdf")
 
-    #: fused-kernel forms (pbr_model.variant): register-resident chunks (A <= 4) or bead-parallel
-    #: records + row teams (A <= 8); 0 lets the library choose
-    VARIANT_AUTO, VARIANT_CHUNK, VARIANT_TEAM = 0, 1, 2
+    #: fused-kernel forms (pbr_model.variant): register-resident chunks (A <= 4), bead-parallel
+    #: records + row teams (A <= 8), or row teams fed by the tensor-core quadratic contraction
+    #: (pbr_sample_eval_tc, precision 32); 0 lets the library choose
+    VARIANT_AUTO, VARIANT_CHUNK, VARIANT_TEAM, VARIANT_TC = 0, 1, 2, 3
+
+    #: auto choice of the tensor-core form: when the quadratic coupling table of the fused forms
+    #: (npair(N) x align4(npair(A)) FP32 values, held in shared memory) exceeds this many bytes
+    TC_TABLE_BYTES = 64 * 1024
+    #: q and V bytes per chunk of the tensor-core form (L2-resident between its launches)
+    TC_CHUNK_BYTES = 64 << 20
 
     def __init__(self, prep, precision=32, device=None, variant=0):
         from . import _native
@@ -259,3 +266,23 @@ class DevicePlan:
             setattr(m, k, self.tensors[k].data_ptr())
         self.struct = m
         self.log_c0 = tabs["log_c0"]
+        self.variant = variant
+        n2, a2p = prep.N * (prep.N + 1) // 2, (prep.A * (prep.A + 1) // 2 + 3) // 4 * 4
+        self.use_tc = precision == 32 and (variant == self.VARIANT_TC or (
+            variant == self.VARIANT_AUTO and n2 * a2p * 4 > self.TC_TABLE_BYTES))
+        self._tc_scratch = None
+
+    def tc_scratch(self):
+        """Device scratch of the tensor-core form (allocated once per plan)."""
+        if self._tc_scratch is None:
+            from . import _native
+            torch = _native.require_cuda()
+            lib = _native.load()
+            prep = self.prep
+            a2p = (prep.A * (prep.A + 1) // 2 + 15) // 16 * 16
+            per = 4 * prep.P * (prep.N + a2p)
+            chunk = max(1, self.TC_CHUNK_BYTES // per)
+            nbytes = int(lib.pbr_sample_eval_tc_scratch(self.struct, chunk))
+            assert nbytes > 0
+            self._tc_scratch = torch.empty(nbytes, dtype=torch.uint8, device=self.tensors["vib_qq"].device)
+        return self._tc_scratch
