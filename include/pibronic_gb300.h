@@ -27,6 +27,7 @@ extern "C" {
 
 /* ---- limits of the fused kernels ---------------------------------------------------------- */
 #define PBR_MAX_A      8        /* surfaces of the coupled model (fused kernels)            */
+#define PBR_MAX_A_WIDE 16       /* surfaces of the coupled model (pbr_sample_eval_tc)        */
 #define PBR_MAX_A_RHO  16       /* surfaces of the sampling model                            */
 #define PBR_MAX_N      64       /* modes                                                    */
 #define PBR_MAX_P      1024     /* beads                                                    */
@@ -119,15 +120,14 @@ int pbr_sample_eval(const pbr_model* model, uint64_t seed, uint64_t offset, int6
                     const pbr_outputs* out, void* stream);
 
 /*
- * The same block evaluation with the quadratic coupling contraction on the tensor cores, for
- * large N (precision 32 only): per chunk of samples the sampler writes q (into out->q_out when
- * given, else into scratch), the tcgen05 contraction (TF32, hi/lo split, three MMAs per K step)
- * writes the quadratic part of V for every (sample, bead) row, and the row-team kernel evaluates
- * the chunk from q and that V.  Draws the same samples as pbr_sample_eval for the same seed and
+ * The same block evaluation with the potential V(q) built on the tensor cores, for large N
+ * (precision 32 only): per chunk of samples the sampler writes q (into out->q_out when given,
+ * else into scratch), the tcgen05 GEMM (TF32, hi/lo split, three MMAs per K step) writes V for
+ * every (sample, bead) row, and the row-team kernel evaluates the chunk from q and that V.  Draws the same samples as pbr_sample_eval for the same seed and
  * offset.  scratch (256-byte aligned, scratch_bytes long) bounds the chunk:
  * pbr_sample_eval_tc_scratch(model, chunk) is the size for a chunk of that many samples; a
  * scratch too small for one sample gives PBR_ERR_CAPACITY.  Replaces the same reference stages
- * as pbr_sample_eval (the quadratic term is pimc.py:1147).
+ * as pbr_sample_eval (V is pimc.py:1145-1150).
  */
 int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk);
 int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X,
@@ -366,21 +366,26 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
                 int32_t* status, void* stream);
 
 /*
- * The quadratic coupling contraction alone (the middle stage of pbr_sample_eval_tc), for tests and
- * custom pipelines.  pbr_tc_quadratic_dims gives the padded K extent n2p (pairs d >= e of modes,
- * a multiple of 32) and column count a2p (pairs b >= c of surfaces, a multiple of 16).
- * pbr_tc_pack_quadratic turns vib_qq ([N(N+1)/2][A(A+1)/2], FP32 or FP64 as precision says) into
- * the TF32 hi / lo operands b_hi, b_lo [a2p][n2p] (16-byte aligned).  pbr_tc_quadratic writes
- * vq [X * P][a2p] (FP32; row sample * P + bead, column pair_index(b, c)) =
- * sum_{d >= e} q_d q_e vib_qq[pair_index(d, e)][pair_index(b, c)] from q [X][N][P] (FP32).
- * Waits are bounded as in pbr_tc_gemm.  Replaces pimc.py:1147 (the quadratic einsum of
- * build_denominator / build_numerator's V).
+ * The diabatic potential alone (the middle stage of pbr_sample_eval_tc), for tests and custom
+ * pipelines: V(q) = E + sum_j L_j q_j + sum_{d >= e} Qp_de q_d q_e as one tcgen05 GEMM (TF32 hi/lo
+ * split, three MMAs per K step, FP32 accumulation in TMEM).  K is laid out in quads of four
+ * columns (d, e0..e0+3) over the bead row's slots s = [q_0..q_{N-1}, 0 up to NA = N rounded up to
+ * 4, 1, 0, 0, 0]: quads (d < N, e0 = 0, 4, .. <= d) hold the pairs e <= d, quads (NA, j0) the
+ * linear terms, quad (NA, NA) the energies, quads (NA + 1, NA) pad to a multiple of 32.
+ * pbr_tc_potential_dims gives the padded K extent n2p and the column count a2p (A(A+1)/2 rounded up
+ * to 16).  pbr_tc_pack_potential turns vib_qq [N(N+1)/2][A(A+1)/2], vib_l [N][A(A+1)/2] and vib_e
+ * [A(A+1)/2] (FP32 or FP64 as precision says; vib_l and vib_e nullable = zero) into b_packed
+ * (2 * a2p * n2p floats, 16-byte aligned): per stage of 32 K columns, the TF32 hi part then the lo
+ * part, each a2p rows x 8 cores of 4 columns, core (row r, core c) at ((r/8)*8 + c)*8 + r%8 in
+ * 16-byte units.  pbr_tc_potential writes vq [X * P][a2p] (FP32; row sample * P + bead, column
+ * pair_index(b, c)) from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in
+ * pbr_tc_gemm.  Replaces pimc.py:1145-1150 (V of diagonalize_coupling_matrix).
  */
-int pbr_tc_quadratic_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
-int pbr_tc_pack_quadratic(const void* vib_qq, int32_t precision, int32_t N, int32_t A, float* b_hi,
-                          float* b_lo, void* stream);
-int pbr_tc_quadratic(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const float* b_hi,
-                     const float* b_lo, float* vq, int32_t* status, void* stream);
+int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
+int pbr_tc_pack_potential(const void* vib_qq, const void* vib_l, const void* vib_e, int32_t precision,
+                          int32_t N, int32_t A, void* b_packed, void* stream);
+int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const void* b_packed,
+                     float* vq, int32_t* status, void* stream);
 
 /* Library version string and the SM architecture it was built for. */
 const char* pbr_version(void);

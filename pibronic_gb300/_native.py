@@ -33,7 +33,7 @@ EXPORTED = (
     "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
     "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
     "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
-    "pbr_tc_gemm", "pbr_tc_quadratic_dims", "pbr_tc_pack_quadratic", "pbr_tc_quadratic",
+    "pbr_tc_gemm", "pbr_tc_potential_dims", "pbr_tc_pack_potential", "pbr_tc_potential",
     "pbr_sample_eval_tc_scratch", "pbr_sample_eval_tc", "pbr_version",
 )
 
@@ -118,9 +118,9 @@ def _declare(lib):
         "pbr_reduce_jackknife_segments": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp]),
         "pbr_reduce_segments_scratch": (i64, [i32]),
         "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
-        "pbr_tc_quadratic_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
-        "pbr_tc_pack_quadratic": (C.c_int, [vp, i32, i32, i32, vp, vp, vp]),
-        "pbr_tc_quadratic": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, vp]),
+        "pbr_tc_potential_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
+        "pbr_tc_pack_potential": (C.c_int, [vp, vp, vp, i32, i32, i32, vp, vp]),
+        "pbr_tc_potential": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp]),
         "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),
         "pbr_sample_eval_tc": (C.c_int, [C.POINTER(PbrModel), u64, u64, i64, C.POINTER(PbrOutputs), vp, i64, vp]),
         "pbr_version": (C.c_char_p, []),
@@ -129,6 +129,31 @@ def _declare(lib):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+
+
+class _StrictLibrary:
+    """The ctypes library with every declared entry point checked for its argument count: ctypes
+    itself passes surplus arguments on silently, which would turn a stale call into a wrong
+    pointer (a stream handle, say) inside the library."""
+
+    def __init__(self, lib):
+        self._lib = lib
+        self._cache = {}
+
+    def __getattr__(self, name):
+        fn = self._cache.get(name)
+        if fn is None:
+            raw = getattr(self._lib, name)
+            nargs = len(raw.argtypes) if raw.argtypes is not None else None
+
+            def fn(*args, _raw=raw, _n=nargs, _name=name):
+                if _n is not None and len(args) != _n:
+                    raise TypeError(f"{_name} takes {_n} arguments ({len(args)} given)")
+                return _raw(*args)
+
+            fn.raw = raw
+            self._cache[name] = fn
+        return fn
 
 
 def load(path=None):
@@ -146,8 +171,8 @@ def load(path=None):
         if missing:
             raise RuntimeError(f"{path} lacks symbols {missing}")
         _declare(lib)
-        _LIB = lib
-        return lib
+        _LIB = _StrictLibrary(lib)
+        return _LIB
 
 
 def check(status, what):

@@ -3,6 +3,7 @@
 #include <cstring>
 
 #include "pbr_team.cuh"
+#include "pbr_wide.cuh"
 
 namespace pbr {
 template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
@@ -10,9 +11,10 @@ template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
 template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, cudaStream_t);
 int tc_quadratic_cols(int A);
 int tc_quadratic_kdim(int N);
-int tc_quadratic_launch(const float*, int64_t, int, int, int, const float*, const float*, int, float*, int32_t*,
-                        cudaStream_t);
-int tc_pack_launch(const void*, int, int, int, float*, float*, cudaStream_t);
+int tc_quadratic_launch(const float*, int64_t, int, int, int, const void*, float*, int32_t*, cudaStream_t);
+int tc_pack_launch(const void*, const void*, const void*, int, int, int, void*, cudaStream_t);
+extern template int launch_wide<12>(int, const WideArgs&, cudaStream_t);   // pbr_wide_a12.cu
+extern template int launch_wide<16>(int, const WideArgs&, cudaStream_t);   // pbr_wide_a16.cu
 }
 
 namespace {
@@ -93,9 +95,9 @@ int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_
     }
 }
 
-int check_model(const pbr_model& m, int qmode, const void* q_in, const pbr_outputs* out) {
+int check_model(const pbr_model& m, int qmode, const void* q_in, const pbr_outputs* out, int max_a = PBR_MAX_A) {
     using namespace pbr;
-    if (m.A < 1 || m.A > PBR_MAX_A) return PBR_ERR_UNSUPPORTED;
+    if (m.A < 1 || m.A > max_a) return PBR_ERR_UNSUPPORTED;
     if (m.variant < 0 || m.variant > 3) return PBR_ERR_ARG;
     if (m.A_rho < m.A || m.A_rho > PBR_MAX_A_RHO) return PBR_ERR_ARG;
     if (m.n_fill_rho != m.A) return PBR_ERR_ARG;
@@ -210,10 +212,21 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
         if (bytes <= kMaxSmem || a.G == 32) break;
         a.G *= 2;
     }
-    if (bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (bytes > kMaxSmem) {
+        // samples too large to stage whole in shared memory: the row-streaming form
+        if (m.precision != 32) return PBR_ERR_UNSUPPORTED;
+        int dev = 0, sms = 0;
+        PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
+        PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int64_t warps = (X + 31) / 32 * m.N;
+        const int64_t blocks = (warps + kRowsWarps - 1) / kRowsWarps;
+        const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(sms) * 8));
+        sample_q_rows_kernel<float><<<grid, kRowsWarps * 32, 0, st>>>(a);
+        return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+    }
     a.logG = ilog2(a.G);
     a.C = (m.P + a.G - 1) / a.G;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     auto go = [&](auto kern) -> int {
         if (bytes > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
@@ -343,7 +356,26 @@ int64_t align_bytes(int64_t n) { return (n + kScratchAlign - 1) / kScratchAlign 
 
 int64_t tc_fixed_bytes(const pbr_model& m) {
     const int64_t b = static_cast<int64_t>(pbr::tc_quadratic_cols(m.A)) * pbr::tc_quadratic_kdim(m.N) * 4;
-    return 2 * align_bytes(b) + kScratchAlign;
+    return align_bytes(2 * b) + kScratchAlign;
+}
+
+// The wide form's tile: up to 16 teams per sample, windows of up to 8 beads per team.
+int run_wide(const pbr_model& m, const float* q, const float* vq, int ld, int64_t X, const pbr_outputs* out,
+             cudaStream_t st) {
+    using namespace pbr;
+    WideArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.m = m;
+    a.q = q;
+    a.vq = vq;
+    a.vq_ld = ld;
+    a.X = X;
+    a.out = *out;
+    a.G = std::min(kWideTeams, m.P);
+    a.C = (m.P + a.G - 1) / a.G;
+    a.W = std::min(a.C, 8);
+    if (m.A <= 12) return launch_wide<12>(m.K, a, st);
+    return launch_wide<16>(m.K, a, st);
 }
 
 int64_t tc_sample_bytes(const pbr_model& m) {
@@ -355,7 +387,7 @@ int64_t tc_sample_bytes(const pbr_model& m) {
 extern "C" {
 
 int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk) {
-    if (!model || chunk < 1 || model->A < 1 || model->A > PBR_MAX_A || model->N < 1 || model->N > PBR_MAX_N ||
+    if (!model || chunk < 1 || model->A < 1 || model->A > PBR_MAX_A_WIDE || model->N < 1 || model->N > PBR_MAX_N ||
         model->P < 3 || model->P > PBR_MAX_P)
         return -1;
     return tc_fixed_bytes(*model) + 2 * kScratchAlign + chunk * tc_sample_bytes(*model);
@@ -367,9 +399,10 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
     if (!model || !out || X < 0 || !scratch) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const pbr_model& m = *model;
-    const int chk = check_model(m, kSample, nullptr, out);
+    const int chk = check_model(m, kSample, nullptr, out, PBR_MAX_A_WIDE);
     if (chk != PBR_OK) return chk;
     if (m.precision != 32) return PBR_ERR_UNSUPPORTED;        // TF32 split: the FP32 form only
+    const bool wide = m.A > PBR_MAX_A;
     if (reinterpret_cast<uintptr_t>(scratch) % kScratchAlign) return PBR_ERR_ARG;
     const int64_t per = tc_sample_bytes(m);
     const int64_t chunk = (scratch_bytes - tc_fixed_bytes(m) - 2 * kScratchAlign) / per;
@@ -377,13 +410,11 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int A2P = tc_quadratic_cols(m.A), N2P = tc_quadratic_kdim(m.N);
     unsigned char* base = static_cast<unsigned char*>(scratch);
-    const int64_t bbytes = align_bytes(static_cast<int64_t>(A2P) * N2P * 4);
-    float* b_hi = reinterpret_cast<float*>(base);
-    float* b_lo = reinterpret_cast<float*>(base + bbytes);
+    void* bpack = base;
     float* qbuf = reinterpret_cast<float*>(base + tc_fixed_bytes(m));
     float* vq = reinterpret_cast<float*>(base + tc_fixed_bytes(m) +
                                          align_bytes(chunk * static_cast<int64_t>(m.N) * m.P * 4));
-    int rc = tc_pack_launch(m.vib_qq, m.precision, m.N, m.A, b_hi, b_lo, st);
+    int rc = tc_pack_launch(m.vib_qq, m.vib_l, m.vib_e, m.precision, m.N, m.A, bpack, st);
     if (rc != PBR_OK) return rc;
     const int K1 = m.K + 1;
     for (int64_t c0 = 0; c0 < X; c0 += chunk) {
@@ -392,7 +423,7 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
         rc = pbr_sample_q(model, seed, offset + static_cast<uint64_t>(c0), n, qc,
                           out->src_out ? out->src_out + c0 : nullptr, stream);
         if (rc != PBR_OK) return rc;
-        rc = tc_quadratic_launch(qc, n, m.N, m.P, A2P, b_hi, b_lo, N2P, vq, out->status, st);
+        rc = tc_quadratic_launch(qc, n, m.N, m.P, A2P, bpack, vq, out->status, st);
         if (rc != PBR_OK) return rc;
         pbr_outputs oc = *out;
         oc.s_rho = out->s_rho + c0;
@@ -403,7 +434,7 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
         oc.log_scale = out->log_scale ? out->log_scale + c0 : nullptr;
         oc.q_out = nullptr;
         oc.src_out = nullptr;
-        rc = run_team(m, kQ32V, qc, n, 0, 0, &oc, st, vq, A2P);
+        rc = wide ? run_wide(m, qc, vq, A2P, n, &oc, st) : run_team(m, kQ32V, qc, n, 0, 0, &oc, st, vq, A2P);
         if (rc != PBR_OK) return rc;
     }
     return PBR_OK;

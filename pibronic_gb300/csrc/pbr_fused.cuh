@@ -26,8 +26,8 @@ namespace pbr {
 
 constexpr int kThreads = 128;
 constexpr int kMaxChunk = 8;       // target beads per thread (chunk length) of the ring product
-// kQ32V: q from the caller (FP32) and the quadratic coupling part of V(q) precomputed per
-// (sample, bead) row by the tensor-core contraction (row-team form only)
+// kQ32V: q from the caller (FP32) and V(q) precomputed per (sample, bead) row by the
+// tensor-core contraction (row-team form only)
 enum QMode : int { kSample = 0, kQ64 = 1, kQ32 = 2, kQ32V = 3 };
 
 struct FusedArgs {
@@ -72,6 +72,19 @@ struct SmemPlan {
 };
 
 template <typename T> __device__ __forceinline__ T dev_fabs(T x) { return x < T(0) ? -x : x; }
+
+// CNT consecutive values to shared memory, 128-bit stores for FP32 when CNT % 4 == 0.
+template <typename T, int CNT>
+__device__ __forceinline__ void stv(T* __restrict__ dst, const T (&src)[CNT]) {
+    if constexpr (sizeof(T) == 4 && CNT % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < CNT; i += 4)
+            *reinterpret_cast<float4*>(dst + i) = make_float4(src[i], src[i + 1], src[i + 2], src[i + 3]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < CNT; ++i) dst[i] = src[i];
+    }
+}
 
 // CNT consecutive table values from shared memory, 128-bit loads where the type allows.
 template <typename T, int CNT>
@@ -207,11 +220,12 @@ __device__ __forceinline__ int draw_source(const pbr_model& m, uint64_t sg, uint
 // z_p (Philox counter (j * ceil(P/4) + p/4, sample), Box-Muller) and back substitution
 // x = L^-T z through the cyclic-tridiagonal factor of rho's bead precision,
 //   x_p = a_p (z_p - b_p x_{p+1} - c_p x_{P-1}),  q_p = x_p + d_src,j,
-// written to the sample's shared-memory row (layout qidx).  The distribution is rho's
+// handed to sink(p, q_p) for p = P-1 down to 0.  The FMAs are explicit so every kernel form
+// that draws through this function produces the same bits.  The distribution is rho's
 // N(d_src, Lambda^-1), the one the reference draws in normal modes.
-template <typename T>
-__device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t key0, uint32_t key1,
-                                T dsh, T* qs, int rs) {
+template <typename T, typename Sink>
+__device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, uint64_t sg, uint32_t key0,
+                                                   uint32_t key1, T dsh, Sink&& sink) {
     const int N = m.N, P = m.P;
     const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
     const T* b = a + static_cast<int64_t>(N) * P;
@@ -233,12 +247,19 @@ __device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t
                 x = __ldg(a + p) * T(z[t]);
                 xlast = x;
             } else {
-                x = __ldg(a + p) * (T(z[t]) - __ldg(b + p) * xnext - __ldg(c + p) * xlast);
+                const T u = fma(-__ldg(b + p), xnext, T(z[t]));
+                x = __ldg(a + p) * fma(-__ldg(c + p), xlast, u);
             }
             xnext = x;
-            qs[qidx(j, p, rs)] = x + dsh;
+            sink(p, x + dsh);
         }
     }
+}
+
+template <typename T>
+__device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t key0, uint32_t key1,
+                                T dsh, T* qs, int rs) {
+    draw_mode_chain_to<T>(m, j, sg, key0, key1, dsh, [&](int p, T v) { qs[qidx(j, p, rs)] = v; });
 }
 
 // Phase A on the sampling path of the chunk form: the G threads of one sample (lanes gmask)
@@ -683,6 +704,44 @@ __global__ void __launch_bounds__(kThreads) sample_q_kernel(const FusedArgs args
             }
         }
         __syncwarp();
+    }
+}
+
+// Sampling only, streamed to global memory for any N x P: a warp draws mode j of 32 consecutive
+// samples (lane = sample, so the ring-factor coefficients are broadcast loads), buffers 32 beads
+// per lane in shared memory and writes them back as 128-byte rows of q [X][N][P].
+constexpr int kRowsWarps = 8;
+template <typename T>
+__global__ void __launch_bounds__(kRowsWarps * 32) sample_q_rows_kernel(const FusedArgs args) {
+    __shared__ float buf[kRowsWarps][32][33];
+    const pbr_model& m = args.m;
+    const int N = m.N, P = m.P;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t groups = (args.X + 31) / 32;
+    float (*wb)[33] = buf[warp];
+    for (int64_t wg = static_cast<int64_t>(blockIdx.x) * kRowsWarps + warp; wg < groups * N;
+         wg += static_cast<int64_t>(gridDim.x) * kRowsWarps) {
+        const int j = static_cast<int>(wg % N);
+        const int64_t xb = (wg / N) * 32;
+        const int64_t x = xb + lane;
+        const bool valid = x < args.X;
+        const uint64_t sg = args.offset + static_cast<uint64_t>(valid ? x : xb);
+        const int src = draw_source<T>(m, sg, args.key0, args.key1);
+        if (valid && j == 0 && args.out.src_out) args.out.src_out[x] = src;
+        const T dsh = static_cast<const T*>(m.rho_d)[static_cast<int64_t>(src) * N + j];
+        draw_mode_chain_to<T>(m, j, sg, args.key0, args.key1, dsh, [&](int p, T v) {
+            wb[lane][p & 31] = static_cast<float>(v);
+            if ((p & 31) == 0) {                       // beads p .. p+31 of the 32 rows are complete
+                __syncwarp();
+                const int pe = min(P, p + 32);
+                for (int i = 0; i < 32; ++i) {
+                    const int64_t xi = xb + i;
+                    if (xi < args.X && p + lane < pe)
+                        args.out.q_out[(xi * N + j) * static_cast<int64_t>(P) + p + lane] = wb[i][lane];
+                }
+                __syncwarp();
+            }
+        });
     }
 }
 

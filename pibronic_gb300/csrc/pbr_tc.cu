@@ -215,23 +215,108 @@ extern "C" int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, 
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 // ---------------------------------------------------------------------------------------------
-// The quadratic coupling contraction on tensor cores (pimc.py:1147, the 'acef,debc,abdf->afbc'
-// einsum):  Vq[row][pr] = sum_{k=(d>=e)} (q_d q_e)[row] * Qp[pr][k]   for row = sample * P + bead,
-// pr = pair_index(b, c), k = pair_index(d, e) and Qp[pr][k] the symmetrised 1/2 Q couplings.
+// The diabatic potential on tensor cores (pimc.py:1145-1150: the quadratic 'acef,debc,abdf->afbc'
+// einsum, the linear einsum and the energies) as one GEMM with an extended K dimension:
+//   V[row][pr] = sum_k a[row][k] * Bm[pr][k],   row = sample * P + bead, pr = pair_index(b, c).
+// K is laid out in quads of four columns (d, e0 .. e0+3): a = s_d * s_e over the bead row's
+// slots s = [q_0 .. q_{N-1}, 0 .. (to NA = N rounded up to 4), 1, 0, 0, 0].  Quads (d, e0) for
+// d < N and e0 = 0, 4, .. <= d cover the quadratic pairs e <= d (Bm = the symmetrised 1/2 Q
+// couplings, zero for e > d), quads (NA, j0) the linear terms (Bm = L_e for e < N), quad (NA, NA)
+// the energies (Bm = E at its first column); quads (NA + 1, NA) = 0 pad K to a multiple of 32.
 //
-// TF32 with a hi/lo split of both operands: three MMAs per K step (hi*hi + hi*lo + lo*hi) with
-// FP32 accumulation in TMEM keep about 21 bits of every product, the accuracy of the FP32 FMA
-// form.  The A operand (pair products of the row's bead coordinates) is generated into shared
-// memory stage by stage; the B operand (Qp hi and lo, [A2P][N2P] K-major, packed on the device by
-// pbr_tc_pack_quadratic) is copied per stage from L2.  Two stage buffers: the threads generate
-// stage s+1 while the tensor core multiplies stage s.  A CTA is 256 threads on 128 rows (two
-// threads per row, one per half of the stage's K slice); TMEM lane r holds row r.
+// TF32 with a hi/lo split of both operands: three MMAs per K step (hi*hi + hi*lo + lo*hi), FP32
+// accumulation in TMEM, about 21 bits kept per product (the accuracy of the FP32 FMA form).
+// Warp-specialised persistent CTA, one 128-row tile at a time:
+//   warps 0-7  generate the A operand stage by stage (two threads per row, four quads each: one
+//              broadcast load of q_d, one 128-bit load of q_e0..e0+3, hi / lo by masking to TF32),
+//              then read the finished accumulator out of TMEM and store V;
+//   warp 8     issues the tcgen05.mma of each stage once its A and B operands are in place;
+//   warp 9     streams the B stages (packed on the device in the shared-memory core layout) with
+//              cp.async.bulk; when all stages fit they are loaded once and stay resident.
+// Stage buffers are handed over with mbarriers (full: producers arrived / bytes landed; empty:
+// tcgen05.commit after the MMAs that read them); two TMEM accumulators let the MMAs of one tile
+// run while the previous tile is read out.  Every wait is bounded: on a timeout a CTA records
+// PBR_ERR_CUDA, every role leaves its loop, and the TMEM is freed after a bounded drain.
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-constexpr int kQThreads = 256;
+constexpr int kGenThreads = 256;                      // warps 0-7
+constexpr int kPotThreads = kGenThreads + 64;         // + MMA warp + B-loader warp
 constexpr int kQStageK = 32;                          // TF32 elements of K per stage (128 B)
-constexpr int kQStageBytesA = kBM * kStageBytesK;     // one 128-row operand part of one stage
+constexpr int kQuadsPerStage = kQStageK / 4;
+constexpr int kAStage = kBM * kStageBytesK;           // one 128-row operand part of one stage
+
+// slot of the constant 1 (16-byte aligned), and the row stride of the slots in shared memory:
+// >= NA + 4 and == 4 (mod 8) for conflict-free 128-bit loads by consecutive rows
+__host__ __device__ inline int q_one(int N) { return (N + 3) / 4 * 4; }
+__host__ __device__ inline int q_stride(int N) {
+    int ns = q_one(N) + 4;
+    if (ns % 8 == 0) ns += 4;
+    return ns;
+}
+
+// number of quads before padding, and quad qi -> (d, e0)
+__host__ __device__ inline int quad_count(int N) {
+    int n = 0;
+    for (int d = 0; d < N; ++d) n += (d + 4) / 4;
+    return n + (N + 3) / 4 + 1;
+}
+__host__ __device__ inline void quad_of(int qi, int N, int& d, int& e0) {
+    for (int dd = 0; dd < N; ++dd) {
+        const int n = (dd + 4) / 4;
+        if (qi < n) { d = dd; e0 = 4 * qi; return; }
+        qi -= n;
+    }
+    const int nl = (N + 3) / 4, na = q_one(N);
+    if (qi < nl) { d = na; e0 = 4 * qi; return; }       // linear
+    if (qi == nl) { d = na; e0 = na; return; }          // energies
+    d = na + 1; e0 = na;                                // padding: 0 * [1, 0, 0, 0]
+}
+
+struct PotSmem {
+    int nb, a, b, q, quads, bars, total;
+    __host__ __device__ PotSmem(int N, int A2P, int nst, int nbuf) {
+        nb = nbuf;
+        int o = 0;
+        a = o;     o += nb * 2 * kAStage;                           // [buffer][hi, lo]
+        b = o;     o += nb * 2 * A2P * kStageBytesK;                // [buffer][hi, lo]
+        q = o;     o += kBM * q_stride(N) * 4;
+        quads = o; o += ((nst * kQuadsPerStage * 4 + 15) / 16) * 16;
+        bars = o;  o += (3 * nb + 6) * 8 + 16;                      // barriers, TMEM slot, error flag
+        total = o;
+    }
+};
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}\n"
+                 ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+// 16 consecutive FP32 accumulator columns of this warp's 32 TMEM lanes
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
 __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
@@ -239,188 +324,278 @@ __device__ __forceinline__ float tf32_rna(float x) {
     return __uint_as_float(r);
 }
 
-struct QuadSmem {
-    int a, b, q, pairs, bar, total;
-    __host__ __device__ QuadSmem(int N, int N2P, int A2P) {
-        int o = 0;
-        a = o;     o += 2 * 2 * kQStageBytesA;                // [buffer][hi, lo] A stages
-        b = o;     o += 2 * 2 * A2P * kStageBytesK;           // [buffer][hi, lo] B stages
-        q = o;     o += kBM * (N | 1) * 4;                    // bead coordinates, odd row stride
-        pairs = o; o += ((N2P * 4 + 15) / 16) * 16;           // (d, e) of every K index
-        bar = o;   o += 32;                                   // two mbarriers + the TMEM slot
-        total = o;
+// bounded wait that gives up early once another role has recorded an error
+__device__ __forceinline__ bool mbar_wait_or_err(uint64_t* bar, uint32_t parity, volatile int* err) {
+    const uint32_t a = smem_u32(bar);
+    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+        if ((it & 1023u) == 1023u && *err) return false;
     }
-};
+    *err = 1;
+    return false;
+}
 
-__global__ void __launch_bounds__(kQThreads) tc_quadratic_kernel(
-        const float* __restrict__ q, int64_t X, int N, int P, int N2, int N2P, int A2P,
-        const float* __restrict__ b_hi, const float* __restrict__ b_lo, float* __restrict__ vq, int ncols,
-        int32_t* status) {
+__global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
+        const float* __restrict__ q, int64_t X, int N, int P, int nst, int A2P, int nbuf,
+        const unsigned char* __restrict__ bpack, float* __restrict__ vq, int ncols, int32_t* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
-    const QuadSmem L(N, N2P, A2P);
+    const PotSmem L(N, A2P, nst, nbuf);
+    const int NB = L.nb;
     unsigned char* sa = tsm + L.a;
     unsigned char* sb = tsm + L.b;
     float* sq = reinterpret_cast<float*>(tsm + L.q);
-    int16_t* spair = reinterpret_cast<int16_t*>(tsm + L.pairs);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(tsm + L.bar);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 2);
-    const int NS = N | 1;
+    uint32_t* squad = reinterpret_cast<uint32_t*>(tsm + L.quads);
+    uint64_t* full_a = reinterpret_cast<uint64_t*>(tsm + L.bars);
+    uint64_t* full_b = full_a + NB;
+    uint64_t* empty = full_b + NB;
+    uint64_t* acc_full = empty + NB;
+    uint64_t* acc_empty = acc_full + 2;
+    uint64_t* sq_ready = acc_empty + 2;
+    uint64_t* sq_done = sq_ready + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sq_done + 1);
+    volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const int NS = q_stride(N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int BSTAGE = A2P * kStageBytesK;
+    const uint32_t BSTAGE = static_cast<uint32_t>(A2P) * kStageBytesK;
+    const int64_t rows = X * P;
+    const int64_t tiles = (rows + kBM - 1) / kBM;
+    const int my_tiles = static_cast<int>(tiles > blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0);
+    const bool resident = nst <= NB;
 
-    if (warp == 0) {
+    if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
                      ::"r"(smem_u32(tmem_slot)), "r"(ncols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (tid == 0) { mbar_init(bar, 1); mbar_init(bar + 1, 1); }
-    for (int d = tid; d < N; d += kQThreads)
-        for (int e = 0; e <= d; ++e) {
-            const int k = d * (d + 1) / 2 + e;
-            spair[2 * k] = static_cast<int16_t>(d);
-            spair[2 * k + 1] = static_cast<int16_t>(e);
+    if (tid == 0) {
+        for (int i = 0; i < NB; ++i) {
+            mbar_init(full_a + i, kGenThreads);
+            mbar_init(full_b + i, 1);
+            mbar_init(empty + i, 1);
         }
-    for (int k = N2 + tid; k < N2P; k += kQThreads) { spair[2 * k] = 0; spair[2 * k + 1] = 0; }
+        for (int i = 0; i < 2; ++i) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, kGenThreads); }
+        mbar_init(sq_ready, kGenThreads);
+        mbar_init(sq_done, kGenThreads);
+        *err = 0;
+    }
+    for (int qi = tid; qi < nst * kQuadsPerStage; qi += kPotThreads) {
+        int d, e0;
+        quad_of(qi, N, d, e0);
+        squad[qi] = static_cast<uint32_t>(d) | (static_cast<uint32_t>(e0) << 16);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmem_slot;
-    const uint32_t idesc = instr_desc(2, kBM, A2P);
-    constexpr uint32_t LBO = 128, SBO = (kStageBytesK / 16) * 128;
-    uint32_t phase = 0u;                              // bit b: parity of buffer b's next commit
-    uint32_t pend = 0u;                               // bit b: a commit of buffer b not yet waited for
-    bool ok = true;
-    const int row_l = tid & (kBM - 1), half = tid >> 7;   // this thread's row and K half
-    const int64_t rows = X * P;
-    const int64_t tiles = (rows + kBM - 1) / kBM;
-    const int nst = N2P / kQStageK;
 
-    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int64_t r0 = tile * kBM;
-        for (int i = tid; i < kBM * N; i += kQThreads) {
-            const int rr = i % kBM, j = i / kBM;
-            const int64_t row = r0 + rr;
-            float v = 0.f;
-            if (row < rows) {
-                const int64_t x = row / P;
-                const int p = static_cast<int>(row - x * P);
-                v = q[(x * N + j) * P + p];
-            }
-            sq[rr * NS + j] = v;
-        }
-        __syncthreads();
+    if (warp < 8) {
+        // ======================= A-operand generators and epilogue ============================
+        // No named barriers here: every hand-over is an mbarrier with a bounded wait, and each
+        // warp leaves the tile loop as a whole (warp-uniform ok), so a timeout cannot strand a
+        // thread at a barrier that the others will never reach.
+        const int row_l = tid & (kBM - 1), half = tid >> 7;
+        const int g = row_l >> 3, rr = row_l & 7;
         const float* myq = sq + row_l * NS;
-        for (int st = 0; st < nst; ++st) {
-            const int bf = st & 1;
-            if (pend & (1u << bf)) {               // the MMAs of stage st-2 read this buffer
-                if (ok) ok = mbar_wait(bar + bf, (phase >> bf) & 1u);
-                phase ^= 1u << bf;
-                pend &= ~(1u << bf);
-            }
-            unsigned char* ahi = sa + bf * 2 * kQStageBytesA;
-            unsigned char* alo = ahi + kQStageBytesA;
-            unsigned char* bhi = sb + bf * 2 * BSTAGE;
-            unsigned char* blo = bhi + BSTAGE;
-            const int k0 = st * kQStageK;
-            {
-                const int g = row_l >> 3, rr = row_l & 7;
-#pragma unroll
-                for (int cc = 0; cc < kQStageK / 8; ++cc) {
-                    const int c = half * (kQStageK / 8) + cc;       // 16-byte core column 0..7
-                    float hi[4], lo[4];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int k = k0 + 4 * c + u;
-                        const uint32_t de = *reinterpret_cast<const uint32_t*>(spair + 2 * k);
-                        const float pr = myq[de & 0xFFFF] * myq[de >> 16];
-                        hi[u] = tf32_rna(pr);
-                        lo[u] = tf32_rna(pr - hi[u]);
+        int it = 0;
+        bool ok = true;
+        for (int tl = 0; tl < my_tiles; ++tl) {
+            ok = __all_sync(0xffffffffu, ok && !*err);
+            if (!ok) break;
+            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
+            if (tl > 0) ok = mbar_wait_or_err(sq_done, (tl - 1) & 1, err);      // sq of tile tl-1 read
+            if (ok) {
+                for (int i = tid; i < kBM * N; i += kGenThreads) {
+                    const int r2 = i % kBM, j = i / kBM;
+                    const int64_t row = r0 + r2;
+                    float v = 0.f;
+                    if (row < rows) {
+                        const int64_t x = row / P;
+                        const int p = static_cast<int>(row - x * P);
+                        v = __ldg(q + (x * N + j) * P + p);
                     }
+                    sq[r2 * NS + j] = v;
+                }
+                for (int i = tid; i < kBM * (NS - N); i += kGenThreads) {
+                    const int r2 = i / (NS - N), j = N + i % (NS - N);
+                    sq[r2 * NS + j] = (j == q_one(N)) ? 1.f : 0.f;
+                }
+                mbar_arrive(sq_ready);
+                ok = mbar_wait_or_err(sq_ready, tl & 1, err);
+            }
+            for (int st = 0; st < nst; ++st, ++it) {
+                const int b = it % NB, use = it / NB;
+                if (ok && use > 0) ok = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
+                if (!ok) continue;
+                unsigned char* ahi = sa + b * 2 * kAStage;
+                unsigned char* alo = ahi + kAStage;
+#pragma unroll
+                for (int u = 0; u < kQuadsPerStage / 2; ++u) {
+                    const int c = half * (kQuadsPerStage / 2) + u;          // 16-byte core column
+                    const uint32_t de = squad[st * kQuadsPerStage + c];
+                    const float qd = myq[de & 0xFFFFu];
+                    const float4 qe = *reinterpret_cast<const float4*>(myq + (de >> 16));
+                    const float x0 = qd * qe.x, x1 = qd * qe.y, x2 = qd * qe.z, x3 = qd * qe.w;
+                    const float h0 = tf32_trunc(x0), h1 = tf32_trunc(x1), h2 = tf32_trunc(x2), h3 = tf32_trunc(x3);
                     const int off = ((g * (kStageBytesK / 16) + c) * 8 + rr) * 16;
-                    *reinterpret_cast<float4*>(ahi + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
-                    *reinterpret_cast<float4*>(alo + off) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+                    *reinterpret_cast<float4*>(ahi + off) = make_float4(h0, h1, h2, h3);
+                    *reinterpret_cast<float4*>(alo + off) = make_float4(tf32_trunc(x0 - h0), tf32_trunc(x1 - h1),
+                                                                        tf32_trunc(x2 - h2), tf32_trunc(x3 - h3));
                 }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(full_a + b);
             }
-            for (int i = tid; i < A2P * (kStageBytesK / 16); i += kQThreads) {
-                const int pr = i / (kStageBytesK / 16), c = i - pr * (kStageBytesK / 16);
-                const int off = (((pr >> 3) * (kStageBytesK / 16) + c) * 8 + (pr & 7)) * 16;
-                const int64_t src = static_cast<int64_t>(pr) * N2P + k0 + 4 * c;
-                *reinterpret_cast<float4*>(bhi + off) = __ldg(reinterpret_cast<const float4*>(b_hi + src));
-                *reinterpret_cast<float4*>(blo + off) = __ldg(reinterpret_cast<const float4*>(b_lo + src));
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncthreads();
-            if (tid == 0 && ok) {
-                asm volatile("tcgen05.fence::after_thread_sync;");
-#pragma unroll
-                for (int kk = 0; kk < kQStageK; kk += 8) {
-                    const uint32_t off = static_cast<uint32_t>(kk * 4 / 16) * 128;
-                    const uint64_t dah = smem_desc(smem_u32(ahi) + off, LBO, SBO);
-                    const uint64_t dal = smem_desc(smem_u32(alo) + off, LBO, SBO);
-                    const uint64_t dbh = smem_desc(smem_u32(bhi) + off, LBO, SBO);
-                    const uint64_t dbl = smem_desc(smem_u32(blo) + off, LBO, SBO);
-                    mma_issue<2>(tmem, dah, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
-                    mma_issue<2>(tmem, dah, dbl, idesc, 1u);
-                    mma_issue<2>(tmem, dal, dbh, idesc, 1u);
-                }
-            }
-            if (tid == 0) mma_commit(bar + bf);   // arrives once the MMAs issued so far complete
-            pend |= 1u << bf;
-        }
-        // drain both buffers: the accumulator is final once the last commit has arrived
-#pragma unroll
-        for (int bf = 0; bf < 2; ++bf)
-            if (pend & (1u << bf)) {
-                if (ok) ok = mbar_wait(bar + bf, (phase >> bf) & 1u);
-                phase ^= 1u << bf;
-                pend &= ~(1u << bf);
-            }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        ok = __syncthreads_and(ok) != 0;
-        if (!ok) break;
-        {
+            if (ok) mbar_arrive(sq_done);
+            // epilogue: this warp's 32 rows, every other 16-column chunk
+            const int acc = tl & 1;
+            if (ok) ok = mbar_wait_or_err(acc_full + acc, (tl >> 1) & 1, err);
+            ok = __all_sync(0xffffffffu, ok);       // tcgen05.ld is warp-collective
+            if (!ok) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
             const int lg = warp & 3, ch = warp >> 2;
             const int64_t row = r0 + lg * 32 + lane;
-            for (int c0 = ch * 32; c0 < A2P; c0 += 64) {
-                float v[32];
-                tmem_ld32(tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(c0), v);
+            for (int c0 = ch * 16; c0 < A2P; c0 += 32) {
+                float v[16];
+                tmem_ld16(tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(acc * A2P + c0), v);
                 if (row < rows) {
                     float* dst = vq + row * A2P + c0;
 #pragma unroll
-                    for (int i = 0; i < 32; i += 4)
-                        if (c0 + i < A2P) *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    for (int i = 0; i < 16; i += 4)
+                        *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                 }
             }
+            asm volatile("tcgen05.fence::before_thread_sync;");
+            mbar_arrive(acc_empty + acc);
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
+    } else if (warp == 8) {
+        // ======================= MMA issuer (one thread) =======================================
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(2, kBM, A2P);
+            constexpr uint32_t LBO = 128, SBO = (kStageBytesK / 16) * 128;
+            uint64_t* last = nullptr;                 // barrier and parity of the latest commit
+            uint32_t lastp = 0;
+            int it = 0;
+            for (int tl = 0; tl < my_tiles && !*err; ++tl) {
+                const int acc = tl & 1;
+                if (tl >= 2 && !mbar_wait_or_err(acc_empty + acc, ((tl >> 1) - 1) & 1, err)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t dtm = tmem + static_cast<uint32_t>(acc * A2P);
+                bool ok = true;
+                for (int st = 0; st < nst; ++st, ++it) {
+                    const int b = it % NB, use = it / NB;
+                    if (!mbar_wait_or_err(full_a + b, use & 1, err) ||
+                        !mbar_wait_or_err(full_b + (resident ? st : b), resident ? 0u : (use & 1), err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const unsigned char* ahi = sa + b * 2 * kAStage;
+                    const unsigned char* alo = ahi + kAStage;
+                    const unsigned char* bhi = sb + (resident ? st : b) * 2 * BSTAGE;
+                    const unsigned char* blo = bhi + BSTAGE;
+#pragma unroll
+                    for (int kk = 0; kk < kQStageK; kk += 8) {
+                        const uint32_t off = static_cast<uint32_t>(kk * 4 / 16) * 128;
+                        const uint64_t dah = smem_desc(smem_u32(ahi) + off, LBO, SBO);
+                        const uint64_t dal = smem_desc(smem_u32(alo) + off, LBO, SBO);
+                        const uint64_t dbh = smem_desc(smem_u32(bhi) + off, LBO, SBO);
+                        const uint64_t dbl = smem_desc(smem_u32(blo) + off, LBO, SBO);
+                        mma_issue<2>(dtm, dah, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
+                        mma_issue<2>(dtm, dah, dbl, idesc, 1u);
+                        mma_issue<2>(dtm, dal, dbh, idesc, 1u);
+                    }
+                    mma_commit(empty + b);
+                    last = empty + b;
+                    lastp = use & 1;
+                }
+                if (!ok) break;
+                mma_commit(acc_full + acc);
+                last = acc_full + acc;
+                lastp = (tl >> 1) & 1;
+            }
+            if (*err && last) mbar_wait(last, lastp);          // bounded drain of the MMAs in flight
+        }
+    } else {
+        // ======================= B-stage loader (one thread) ===================================
+        if (lane == 0) {
+            if (resident) {
+                for (int st = 0; st < nst && my_tiles > 0; ++st) {
+                    mbar_expect_tx(full_b + st, 2 * BSTAGE);
+                    bulk_g2s(sb + st * 2 * BSTAGE, bpack + static_cast<int64_t>(st) * 2 * BSTAGE, 2 * BSTAGE,
+                             full_b + st);
+                }
+                if (*err)
+                    for (int st = 0; st < nst && my_tiles > 0; ++st) mbar_wait(full_b + st, 0);   // bounded drain
+            } else {
+                const int total = my_tiles * nst;
+                uint64_t* last = nullptr;
+                uint32_t lastp = 0;
+                for (int it = 0; it < total && !*err; ++it) {
+                    const int b = it % NB, use = it / NB, st = it % nst;
+                    if (use > 0 && !mbar_wait_or_err(empty + b, (use - 1) & 1, err)) break;
+                    mbar_expect_tx(full_b + b, 2 * BSTAGE);
+                    bulk_g2s(sb + b * 2 * BSTAGE, bpack + static_cast<int64_t>(st) * 2 * BSTAGE, 2 * BSTAGE,
+                             full_b + b);
+                    last = full_b + b;
+                    lastp = use & 1;
+                }
+                if (*err && last) mbar_wait(last, lastp);      // bounded drain of the copy in flight
+            }
+        }
     }
-    if (!ok) {
-        // bounded drain of MMAs still in flight before the TMEM is freed
-        for (int bf = 0; bf < 2; ++bf)
-            if (pend & (1u << bf)) mbar_wait(bar + bf, (phase >> bf) & 1u);
-        if (status && tid == 0) atomicMax(status, PBR_ERR_CUDA);
-    }
+    __syncthreads();
+    if (*err && tid == 0 && status) atomicMax(status, PBR_ERR_CUDA);
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
-    if (warp == 0)
+    if (warp == 8)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
-// Qp (FP32 or FP64 [N2][A2], row k = pair_index(d, e)) -> TF32 hi / lo, [A2P][N2P] K-major, zero padded
+// Qp [N2][A2], L [N][A2], E [A2] (FP32 or FP64; L and E nullable = zero) -> TF32 hi / lo in the
+// stage-major shared-memory core layout: stage s = [hi: A2P rows][lo: A2P rows], each row's 32
+// K columns as 8 cores of 4, core (row r, column c) at ((r / 8) * 8 + c) * 8 + r % 8 (16 B units).
 template <typename T>
-__global__ void tc_pack_kernel(const T* __restrict__ qq, int N2, int A2, int N2P, int A2P, float* __restrict__ bh,
-                               float* __restrict__ bl) {
-    const int64_t n = static_cast<int64_t>(A2P) * N2P;
+__global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en, int N,
+                               int A2, int nst, int A2P, float* __restrict__ out) {
+    const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;      // (stage, row, k in stage)
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int pr = static_cast<int>(i / N2P), k = static_cast<int>(i - static_cast<int64_t>(pr) * N2P);
-        const float x = (pr < A2 && k < N2) ? static_cast<float>(qq[static_cast<int64_t>(k) * A2 + pr]) : 0.f;
+        const int st = static_cast<int>(i / (static_cast<int64_t>(A2P) * kQStageK));
+        const int rem = static_cast<int>(i - static_cast<int64_t>(st) * A2P * kQStageK);
+        const int pr = rem / kQStageK, kk = rem - pr * kQStageK;
+        const int qi = st * kQuadsPerStage + kk / 4, u = kk % 4;
+        int d, e0;
+        quad_of(qi, N, d, e0);
+        const int e = e0 + u;
+        float x = 0.f;
+        const int na = q_one(N);
+        if (pr < A2) {
+            if (d < N) {
+                if (e <= d) x = static_cast<float>(qq[static_cast<int64_t>(d * (d + 1) / 2 + e) * A2 + pr]);
+            } else if (d == na && e0 < N) {
+                if (e < N && lin) x = static_cast<float>(lin[static_cast<int64_t>(e) * A2 + pr]);
+            } else if (d == na && e0 == na) {
+                if (u == 0 && en) x = static_cast<float>(en[pr]);
+            }
+        }
         const float h = tf32_rna(x);
-        bh[i] = h;
-        bl[i] = tf32_rna(x - h);
+        const int c = kk / 4;
+        const int64_t base = static_cast<int64_t>(st) * 2 * A2P * kQStageK;
+        const int64_t slot = (static_cast<int64_t>((pr >> 3) * (kStageBytesK / 16) + c) * 8 + (pr & 7)) * 4 + u;
+        out[base + slot] = h;
+        out[base + static_cast<int64_t>(A2P) * kQStageK + slot] = tf32_rna(x - h);
     }
+}
+
+int pot_buffers(int N, int A2P, int nst) {
+    for (int nb = 3; nb >= 2; --nb)
+        if (PotSmem(N, A2P, nst, nb).total <= 227 * 1024) return nb;
+    return 0;
 }
 
 }  // namespace
@@ -428,50 +603,54 @@ __global__ void tc_pack_kernel(const T* __restrict__ qq, int N2, int A2, int N2P
 namespace pbr {
 
 int tc_quadratic_cols(int A) { return (A * (A + 1) / 2 + 15) / 16 * 16; }
-int tc_quadratic_kdim(int N) { return (N * (N + 1) / 2 + kQStageK - 1) / kQStageK * kQStageK; }
+int tc_quadratic_kdim(int N) { return (quad_count(N) + kQuadsPerStage - 1) / kQuadsPerStage * kQStageK; }
 
-int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const float* b_hi, const float* b_lo,
-                        int N2P, float* vq, int32_t* status, cudaStream_t stream) {
-    if (!q || !b_hi || !b_lo || !vq || X < 0 || N < 1 || N > 64 || P < 1) return PBR_ERR_ARG;
-    const int N2 = N * (N + 1) / 2;
-    if (N2P < N2 || N2P % kQStageK != 0 || A2P < 16 || A2P > 256 || A2P % 16 != 0) return PBR_ERR_ARG;
-    if ((reinterpret_cast<uintptr_t>(b_hi) | reinterpret_cast<uintptr_t>(b_lo) | reinterpret_cast<uintptr_t>(vq)) & 15)
-        return PBR_ERR_ARG;
+int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const void* bpack, float* vq,
+                        int32_t* status, cudaStream_t stream) {
+    if (!q || !bpack || !vq || X < 0 || N < 1 || N > 64 || P < 1) return PBR_ERR_ARG;
+    if (A2P < 16 || A2P > 144 || A2P % 16 != 0) return PBR_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(bpack) | reinterpret_cast<uintptr_t>(vq)) & 15) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
+    const int nst = tc_quadratic_kdim(N) / kQStageK;
     int ncols = 32;
-    while (ncols < A2P) ncols <<= 1;
-    const QuadSmem L(N, N2P, A2P);
-    if (L.total > 227 * 1024) return PBR_ERR_UNSUPPORTED;
+    while (ncols < 2 * A2P) ncols <<= 1;
+    const int nb = pot_buffers(N, A2P, nst);
+    if (nb == 0) return PBR_ERR_UNSUPPORTED;
+    const PotSmem L(N, A2P, nst, nb);
     static int configured = 0;
     if (L.total > configured) {
-        if (cudaFuncSetAttribute(tc_quadratic_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+        if (cudaFuncSetAttribute(tc_potential_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
             cudaSuccess)
             return PBR_ERR_UNSUPPORTED;
         configured = 227 * 1024;
     }
-    int dev = 0, sms = 0, occ = 0;
+    int dev = 0, sms = 0;
     PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
     PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, tc_quadratic_kernel, kQThreads, L.total));
-    if (occ < 1) return PBR_ERR_UNSUPPORTED;
-    if (occ * ncols > 512) occ = 512 / ncols;          // TMEM columns of the resident CTAs
     const int64_t tiles = (X * P + kBM - 1) / kBM;
-    const int grid = static_cast<int>(tiles < static_cast<int64_t>(occ) * sms ? tiles : static_cast<int64_t>(occ) * sms);
-    tc_quadratic_kernel<<<grid, kQThreads, L.total, stream>>>(q, X, N, P, N2, N2P, A2P, b_hi, b_lo, vq, ncols,
-                                                              status);
+    // one CTA per SM: at least half the shared memory each, so two CTAs never share an SM's TMEM
+    const int smem = L.total > 116 * 1024 ? L.total : 116 * 1024;
+    const int grid = static_cast<int>(tiles < sms ? tiles : sms);
+    tc_potential_kernel<<<grid, kPotThreads, smem, stream>>>(q, X, N, P, nst, A2P, nb,
+                                                                 static_cast<const unsigned char*>(bpack), vq,
+                                                                 ncols, status);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 
-int tc_pack_launch(const void* qq, int precision, int N, int A, float* b_hi, float* b_lo, cudaStream_t stream) {
-    if (!qq || !b_hi || !b_lo || N < 1 || N > 64 || A < 1 || A > 22) return PBR_ERR_ARG;
-    const int N2 = N * (N + 1) / 2, A2 = A * (A + 1) / 2;
-    const int N2P = tc_quadratic_kdim(N), A2P = tc_quadratic_cols(A);
-    const int64_t n = static_cast<int64_t>(A2P) * N2P;
+int tc_pack_launch(const void* qq, const void* lin, const void* en, int precision, int N, int A, void* bpack,
+                   cudaStream_t stream) {
+    if (!qq || !bpack || N < 1 || N > 64 || A < 1 || A > 16) return PBR_ERR_ARG;
+    const int A2 = A * (A + 1) / 2;
+    const int nst = tc_quadratic_kdim(N) / kQStageK, A2P = tc_quadratic_cols(A);
+    const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;
     const int grid = static_cast<int>((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    float* out = static_cast<float*>(bpack);
     if (precision == 32)
-        tc_pack_kernel<float><<<grid, 256, 0, stream>>>(static_cast<const float*>(qq), N2, A2, N2P, A2P, b_hi, b_lo);
+        tc_pack_kernel<float><<<grid, 256, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
+                                                        static_cast<const float*>(en), N, A2, nst, A2P, out);
     else if (precision == 64)
-        tc_pack_kernel<double><<<grid, 256, 0, stream>>>(static_cast<const double*>(qq), N2, A2, N2P, A2P, b_hi, b_lo);
+        tc_pack_kernel<double><<<grid, 256, 0, stream>>>(static_cast<const double*>(qq), static_cast<const double*>(lin),
+                                                         static_cast<const double*>(en), N, A2, nst, A2P, out);
     else
         return PBR_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
@@ -481,23 +660,23 @@ int tc_pack_launch(const void* qq, int precision, int N, int A, float* b_hi, flo
 
 extern "C" {
 
-int pbr_tc_quadratic_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p) {
-    if (N < 1 || N > 64 || A < 1 || A > 22 || !n2p || !a2p) return PBR_ERR_ARG;
+int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p) {
+    if (N < 1 || N > 64 || A < 1 || A > 16 || !n2p || !a2p) return PBR_ERR_ARG;
     *n2p = pbr::tc_quadratic_kdim(N);
     *a2p = pbr::tc_quadratic_cols(A);
     return PBR_OK;
 }
 
-int pbr_tc_pack_quadratic(const void* vib_qq, int32_t precision, int32_t N, int32_t A, float* b_hi, float* b_lo,
-                          void* stream) {
-    return pbr::tc_pack_launch(vib_qq, precision, N, A, b_hi, b_lo, static_cast<cudaStream_t>(stream));
+int pbr_tc_pack_potential(const void* vib_qq, const void* vib_l, const void* vib_e, int32_t precision, int32_t N,
+                          int32_t A, void* b_packed, void* stream) {
+    return pbr::tc_pack_launch(vib_qq, vib_l, vib_e, precision, N, A, b_packed, static_cast<cudaStream_t>(stream));
 }
 
-int pbr_tc_quadratic(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const float* b_hi,
-                     const float* b_lo, float* vq, int32_t* status, void* stream) {
-    if (A < 1 || A > 22) return PBR_ERR_ARG;
-    return pbr::tc_quadratic_launch(q, X, N, P, pbr::tc_quadratic_cols(A), b_hi, b_lo, pbr::tc_quadratic_kdim(N),
-                                    vq, status, static_cast<cudaStream_t>(stream));
+int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const void* b_packed, float* vq,
+                     int32_t* status, void* stream) {
+    if (A < 1 || A > 16) return PBR_ERR_ARG;
+    return pbr::tc_quadratic_launch(q, X, N, P, pbr::tc_quadratic_cols(A), b_packed, vq, status,
+                                    static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

@@ -35,7 +35,7 @@ struct TeamArgs {
     int rs;         // q row stride (skewed layout, qidx)
     int qstride;    // q elements per sample
     int rl;         // bead record length
-    const float* vq;  // kQ32V: quadratic part of V, row (sample * P + bead), A(A+1)/2 used columns
+    const float* vq;  // kQ32V: V(q) (energies, linear, quadratic), row (sample * P + bead), A(A+1)/2 used columns
     int vq_ld;        // kQ32V: floats per row of vq
 };
 
@@ -242,7 +242,9 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     }
                 }
 #pragma unroll
-                for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
+                if (QM != kQ32V)
+#pragma unroll
+                    for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
             }
             T lmax;
             {
@@ -282,10 +284,10 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
 #pragma unroll
                 for (int pr = 0; pr < A2; pr += 4) {
                     const float4 w = *reinterpret_cast<const float4*>(vr + pr);
-                    v[pr] += T(w.x);
-                    if (pr + 1 < A2) v[pr + 1] += T(w.y);
-                    if (pr + 2 < A2) v[pr + 2] += T(w.z);
-                    if (pr + 3 < A2) v[pr + 3] += T(w.w);
+                    v[pr] = T(w.x);
+                    if (pr + 1 < A2) v[pr + 1] = T(w.y);
+                    if (pr + 2 < A2) v[pr + 2] = T(w.z);
+                    if (pr + 3 < A2) v[pr + 3] = T(w.w);
                 }
             } else {
                 int row = 0;

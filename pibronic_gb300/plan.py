@@ -250,7 +250,9 @@ class DevicePlan:
         from . import _native
         torch = _native.require_cuda()
         assert precision in (32, 64)
-        assert 1 <= prep.A <= 8, "the fused kernels support 1 to 8 coupled surfaces"
+        assert 1 <= prep.A <= 16, "the kernels support 1 to 16 coupled surfaces"
+        assert prep.A <= 8 or (precision == 32 and variant in (self.VARIANT_AUTO, self.VARIANT_TC)), \
+            "9 to 16 surfaces run on the tensor-core form only (precision 32)"
         self.prep, self.precision = prep, precision
         tabs = prep.tables()
         dt = torch.float32 if precision == 32 else torch.float64
@@ -268,7 +270,7 @@ class DevicePlan:
         self.log_c0 = tabs["log_c0"]
         self.variant = variant
         n2, a2p = prep.N * (prep.N + 1) // 2, (prep.A * (prep.A + 1) // 2 + 3) // 4 * 4
-        self.use_tc = precision == 32 and (variant == self.VARIANT_TC or (
+        self.use_tc = precision == 32 and (variant == self.VARIANT_TC or prep.A > 8 or (
             variant == self.VARIANT_AUTO and n2 * a2p * 4 > self.TC_TABLE_BYTES))
         self._tc_scratch = None
 

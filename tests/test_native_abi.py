@@ -38,3 +38,16 @@ def test_product_path_fails_loudly_without_cuda():
         assert "no CPU fallback" in str(err)
     else:
         raise AssertionError("require_cuda must raise without a device")
+
+
+def test_calls_with_a_wrong_argument_count_are_rejected():
+    """ctypes would pass a surplus argument on silently; the loaded library refuses it before
+    anything reaches the native code."""
+    import pytest
+    from pibronic_gb300 import build, _native
+    lib = _native.load(build.build())
+    assert lib.pbr_version() is not None
+    with pytest.raises(TypeError):
+        lib.pbr_version(0)
+    with pytest.raises(TypeError):
+        lib.pbr_reduce_blocks()
