@@ -386,6 +386,9 @@ def run_ours(args):
     # ---- batched uneven models in one graph-captured launch per surface count ----
     if rank == 0 and not args.no_batched:
         line["batched"] = batched_leg(args)
+    # ---- large dense configuration on the tensor-core form (A=12, N=64, P=256) ----
+    if rank == 0 and not args.no_large:
+        line["large"] = large_leg(args)
     # ---- CPU baseline: the oracle port on the host cores, rank 0 at N=1 only ----
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = host_cores()
@@ -471,6 +474,117 @@ def learned_leg(args):
     return out
 
 
+def tf32_cublas_peak(torch):
+    """cuBLAS TF32 dense GEMM throughput measured in this run (8192^3, best of 5, CUDA events):
+    the denominator for the tcgen05 TF32 kernel (MEASURED_PEAKS.json holds the bf16 peak only)."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    c = a @ b
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b, out=c)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    torch.backends.cuda.matmul.allow_tf32 = old
+    del a, b, c
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def large_leg(args):
+    """The large dense configuration: A=12, N=64, P=256, dense Q ~ N(0, 0.001) eV, T=300 K.  V is
+    built by the tcgen05 TF32 GEMM (pbr_sample_eval_tc), exp(-tau V) by the wide form; the
+    learned proposal (flow over 2 ring slots per mode) is trained on the method's own samples."""
+    import ctypes
+    import torch
+    from pibronic_gb300 import _native, constants, pimc, stats, synthetic, vibronic_io
+    from pibronic_gb300.file_structure import FileStructure
+    from pibronic_gb300.flow import FlowProposal
+    from pibronic_gb300.pimc import evaluate_device
+    A, N, P, T = 12, 64, 256, 300.0
+    X = args.large_samples
+    root = tempfile.mkdtemp(prefix="pbr_large_")
+    FS = FileStructure(root, 0, 0)
+    model = synthetic.make_coupled_model(A, N, 5, sd_quadratic=0.001)
+    vibronic_io.save_model_to_JSON(FS.path_vib_model, model)
+    vibronic_io.create_basic_diagonal_model(FS)
+    data = pimc.BoxDataPM(1e-4 * constants.beta(T))
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.states, data.modes, data.beads, data.temperature = A, N, P, T
+    data.samples = data.block_size = 1000
+    data.blocks = 1
+    data.preprocess()
+    plan = data.plan
+    assert plan.use_tc
+    evaluate_device(plan, 1000, seed=9, offset=0)
+    plain, tp = _timed(torch, lambda: evaluate_device(plan, X, seed=1, offset=0, want_q=True))
+    ep = stats.device_estimates(plain["s_rho"], plain["s_g"], plain["s_gp"], plain["s_gm"], T, data.delta_beta)
+    # the tcgen05 GEMM alone on one L2-sized chunk of this run's q
+    lib = _native.load()
+    n2p, a2p = ctypes.c_int32(), ctypes.c_int32()
+    _native.check(lib.pbr_tc_potential_dims(N, A, ctypes.byref(n2p), ctypes.byref(a2p)), "dims")
+    n2p, a2p = n2p.value, a2p.value
+    Xc = min(X, max(1, (64 << 20) // (4 * P * (N + a2p))))
+    bp = torch.empty(2 * a2p * n2p, dtype=torch.float32, device="cuda")
+    vq = torch.empty((Xc * P, a2p), dtype=torch.float32, device="cuda")
+    t_ = plan.tensors
+    sh = _native.stream_handle()
+    _native.check(lib.pbr_tc_pack_potential(t_["vib_qq"].data_ptr(), t_["vib_l"].data_ptr(), t_["vib_e"].data_ptr(),
+                                            32, N, A, _native.ptr(bp), sh), "pack")
+    qc = plain["q"][:Xc]
+    ts = []
+    for i in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _native.check(lib.pbr_tc_potential(_native.ptr(qc), Xc, N, P, A, _native.ptr(bp), _native.ptr(vq), None, sh),
+                      "tc potential")
+        e1.record()
+        e1.synchronize()
+        if i:
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+    t_tc = min(ts)
+    issued = 6.0 * Xc * P * a2p * n2p / t_tc / 1e12
+    useful = 2.0 * Xc * P * (A * (A + 1) // 2) * (N * (N + 1) // 2 + N + 1) / t_tc / 1e12
+    peak = tf32_cublas_peak(torch)
+
+    def summary(e, t):
+        rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
+               "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
+        sps = X / t
+        return {"samples_per_s": sps, "ess_per_sample": e["ESS"] / X, "ess_per_s": e["ESS"] / t,
+                "Z": e["Z"], "Z error": e["Z error"], "E": e["jk_E"], "E error": e["jk_E error"],
+                "Cv": e["jk_Cv"], "Cv error": e["jk_Cv error"],
+                "time_to_1e-3_s": {k: X * (v / 1e-3) ** 2 / sps for k, v in rel.items()}}
+    out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K dense Q N(0,0.001) eV, dbeta=1e-4 beta, {X} samples",
+           "plain": summary(ep, tp),
+           "tc_gemm": {"chunk_samples": Xc, "ms": 1e3 * t_tc, "issued_tflops": issued, "useful_tflops": useful,
+                       "tf32_cublas_tflops_measured": peak, "frac_of_measured_tf32": issued / peak,
+                       "note": "issued = 3 TF32 passes (hi/lo split) x padded K and columns"}}
+    if not args.no_learned:
+        fl = FlowProposal(data.prepared, plan, nsel=2, layers=8, hidden=128, seed=0)
+        y, _ = fl.prepare(plain["q"])
+        r = plain["s_g"] / plain["s_rho"]
+        del plain["q"]
+        _, t_train = _timed(torch, lambda: fl.train(y, r, epochs=6, batch=16384, lr=1e-3))
+        del y
+        fl.sample_and_evaluate(1000, seed=5)
+        res, tf = _timed(torch, lambda: fl.sample_and_evaluate(X, seed=8))
+        ef = stats.device_estimates(res["s_q"], res["s_g"], res["s_gp"], res["s_gm"], T, data.delta_beta)
+        sl = summary(ef, tf)
+        sp = out["plain"]
+        out["learned"] = sl
+        out["train_s"] = t_train
+        out["ess_per_s_ratio"] = sl["ess_per_s"] / sp["ess_per_s"]
+        out["agreement_sigma"] = {k: abs(sl[k] - sp[k]) / math.hypot(sl[k + " error"], sp[k + " error"])
+                                  for k in ("Z", "E", "Cv")}
+    return out
+
+
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
     each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
@@ -515,6 +629,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-models", type=int, default=256)
     ap.add_argument("--batch-samples", type=int, default=100_000)
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--large-samples", type=int, default=400_000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -133,6 +133,12 @@ int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk);
 int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X,
                        const pbr_outputs* out, void* scratch, int64_t scratch_bytes, void* stream);
 
+/* As pbr_sample_eval_tc on caller-supplied FP32 bead coordinates q [X * N * P] (the learned
+ * proposal's samples at large N or more than 8 surfaces); the sampler stage is skipped.
+ * Replaces pimc.py:1430-1449 for given data.qTensor, as pbr_eval_q_f32. */
+int pbr_eval_q_tc(const pbr_model* model, const float* q, int64_t X, const pbr_outputs* out,
+                  void* scratch, int64_t scratch_bytes, void* stream);
+
 /*
  * Many independent models in one launch per surface count (the batched configuration): every
  * model keeps its own sizes, temperature, seed, counter offset and outputs.  pbr_batch_pack fills

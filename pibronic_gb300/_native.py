@@ -34,7 +34,7 @@ EXPORTED = (
     "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
     "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
     "pbr_tc_gemm", "pbr_tc_potential_dims", "pbr_tc_pack_potential", "pbr_tc_potential",
-    "pbr_sample_eval_tc_scratch", "pbr_sample_eval_tc", "pbr_version",
+    "pbr_sample_eval_tc_scratch", "pbr_sample_eval_tc", "pbr_eval_q_tc", "pbr_version",
 )
 
 
@@ -123,6 +123,7 @@ def _declare(lib):
         "pbr_tc_potential": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp]),
         "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),
         "pbr_sample_eval_tc": (C.c_int, [C.POINTER(PbrModel), u64, u64, i64, C.POINTER(PbrOutputs), vp, i64, vp]),
+        "pbr_eval_q_tc": (C.c_int, [C.POINTER(PbrModel), vp, i64, C.POINTER(PbrOutputs), vp, i64, vp]),
         "pbr_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

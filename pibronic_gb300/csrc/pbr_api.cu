@@ -393,13 +393,19 @@ int64_t pbr_sample_eval_tc_scratch(const pbr_model* model, int64_t chunk) {
     return tc_fixed_bytes(*model) + 2 * kScratchAlign + chunk * tc_sample_bytes(*model);
 }
 
-int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X, const pbr_outputs* out,
-                       void* scratch, int64_t scratch_bytes, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// the chunked tensor-core pipeline; q_in == nullptr: draw q with the sampler
+int run_tc(const pbr_model* model, const float* q_in, uint64_t seed, uint64_t offset, int64_t X,
+           const pbr_outputs* out, void* scratch, int64_t scratch_bytes, void* stream) {
     using namespace pbr;
     if (!model || !out || X < 0 || !scratch) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const pbr_model& m = *model;
-    const int chk = check_model(m, kSample, nullptr, out, PBR_MAX_A_WIDE);
+    const int chk = q_in ? check_model(m, kQ32, q_in, out, PBR_MAX_A_WIDE)
+                         : check_model(m, kSample, nullptr, out, PBR_MAX_A_WIDE);
     if (chk != PBR_OK) return chk;
     if (m.precision != 32) return PBR_ERR_UNSUPPORTED;        // TF32 split: the FP32 form only
     const bool wide = m.A > PBR_MAX_A;
@@ -408,7 +414,7 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
     const int64_t chunk = (scratch_bytes - tc_fixed_bytes(m) - 2 * kScratchAlign) / per;
     if (chunk < 1) return PBR_ERR_CAPACITY;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const int A2P = tc_quadratic_cols(m.A), N2P = tc_quadratic_kdim(m.N);
+    const int A2P = tc_quadratic_cols(m.A);
     unsigned char* base = static_cast<unsigned char*>(scratch);
     void* bpack = base;
     float* qbuf = reinterpret_cast<float*>(base + tc_fixed_bytes(m));
@@ -417,12 +423,19 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
     int rc = tc_pack_launch(m.vib_qq, m.vib_l, m.vib_e, m.precision, m.N, m.A, bpack, st);
     if (rc != PBR_OK) return rc;
     const int K1 = m.K + 1;
+    const int64_t NP = static_cast<int64_t>(m.N) * m.P;
     for (int64_t c0 = 0; c0 < X; c0 += chunk) {
         const int64_t n = std::min(chunk, X - c0);
-        float* qc = out->q_out ? out->q_out + c0 * static_cast<int64_t>(m.N) * m.P : qbuf;
-        rc = pbr_sample_q(model, seed, offset + static_cast<uint64_t>(c0), n, qc,
-                          out->src_out ? out->src_out + c0 : nullptr, stream);
-        if (rc != PBR_OK) return rc;
+        const float* qc;
+        if (q_in) {
+            qc = q_in + c0 * NP;
+        } else {
+            float* qs = out->q_out ? out->q_out + c0 * NP : qbuf;
+            rc = pbr_sample_q(model, seed, offset + static_cast<uint64_t>(c0), n, qs,
+                              out->src_out ? out->src_out + c0 : nullptr, stream);
+            if (rc != PBR_OK) return rc;
+            qc = qs;
+        }
         rc = tc_quadratic_launch(qc, n, m.N, m.P, A2P, bpack, vq, out->status, st);
         if (rc != PBR_OK) return rc;
         pbr_outputs oc = *out;
@@ -438,6 +451,21 @@ int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, i
         if (rc != PBR_OK) return rc;
     }
     return PBR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pbr_sample_eval_tc(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t X, const pbr_outputs* out,
+                       void* scratch, int64_t scratch_bytes, void* stream) {
+    return run_tc(model, nullptr, seed, offset, X, out, scratch, scratch_bytes, stream);
+}
+
+int pbr_eval_q_tc(const pbr_model* model, const float* q, int64_t X, const pbr_outputs* out, void* scratch,
+                  int64_t scratch_bytes, void* stream) {
+    if (!q) return PBR_ERR_ARG;
+    return run_tc(model, q, 0, 0, X, out, scratch, scratch_bytes, stream);
 }
 
 }  // extern "C"

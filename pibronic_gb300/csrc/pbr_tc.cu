@@ -227,12 +227,13 @@ extern "C" int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, 
 // TF32 with a hi/lo split of both operands: three MMAs per K step (hi*hi + hi*lo + lo*hi), FP32
 // accumulation in TMEM, about 21 bits kept per product (the accuracy of the FP32 FMA form).
 // Warp-specialised persistent CTA, one 128-row tile at a time:
-//   warps 0-7  generate the A operand stage by stage (two threads per row, four quads each: one
-//              broadcast load of q_d, one 128-bit load of q_e0..e0+3, hi / lo by masking to TF32),
-//              then read the finished accumulator out of TMEM and store V;
-//   warp 8     issues the tcgen05.mma of each stage once its A and B operands are in place;
-//   warp 9     streams the B stages (packed on the device in the shared-memory core layout) with
-//              cp.async.bulk; when all stages fit they are loaded once and stay resident.
+//   warps 0-7   generate the A operand stage by stage (two threads per row, four quads each: one
+//               broadcast load of q_d, one 128-bit load of q_e0..e0+3, hi / lo by masking to TF32)
+//               from the tile's bead coordinates, which they prefetch one tile ahead (cp.async);
+//   warp 8      issues the tcgen05.mma of each stage once its A and B operands are in place;
+//   warp 9      streams the B stages (packed on the device in the shared-memory core layout) with
+//               cp.async.bulk; when all stages fit they are loaded once and stay resident;
+//   warps 10-13 read the finished accumulator out of TMEM and store V while the next tile runs.
 // Stage buffers are handed over with mbarriers (full: producers arrived / bytes landed; empty:
 // tcgen05.commit after the MMAs that read them); two TMEM accumulators let the MMAs of one tile
 // run while the previous tile is read out.  Every wait is bounded: on a timeout a CTA records
@@ -241,7 +242,8 @@ extern "C" int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, 
 namespace {
 
 constexpr int kGenThreads = 256;                      // warps 0-7
-constexpr int kPotThreads = kGenThreads + 64;         // + MMA warp + B-loader warp
+constexpr int kEpiThreads = 128;                      // warps 10-13
+constexpr int kPotThreads = kGenThreads + 64 + kEpiThreads;   // + MMA warp, B-loader warp, epilogue
 constexpr int kQStageK = 32;                          // TF32 elements of K per stage (128 B)
 constexpr int kQuadsPerStage = kQStageK / 4;
 constexpr int kAStage = kBM * kStageBytesK;           // one 128-row operand part of one stage
@@ -280,7 +282,7 @@ struct PotSmem {
         int o = 0;
         a = o;     o += nb * 2 * kAStage;                           // [buffer][hi, lo]
         b = o;     o += nb * 2 * A2P * kStageBytesK;                // [buffer][hi, lo]
-        q = o;     o += kBM * q_stride(N) * 4;
+        q = o;     o += 2 * kBM * q_stride(N) * 4;                  // two tiles of bead coordinates
         quads = o; o += ((nst * kQuadsPerStage * 4 + 15) / 16) * 16;
         bars = o;  o += (3 * nb + 6) * 8 + 16;                      // barriers, TMEM slot, error flag
         total = o;
@@ -378,10 +380,14 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
             mbar_init(full_b + i, 1);
             mbar_init(empty + i, 1);
         }
-        for (int i = 0; i < 2; ++i) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, kGenThreads); }
+        for (int i = 0; i < 2; ++i) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, kEpiThreads); }
         mbar_init(sq_ready, kGenThreads);
         mbar_init(sq_done, kGenThreads);
         *err = 0;
+    }
+    for (int i = tid; i < 2 * kBM * (NS - N); i += kPotThreads) {      // the constant slots of both tiles
+        const int r2 = i / (NS - N), j = N + i % (NS - N);
+        sq[r2 * NS + j] = (j == q_one(N)) ? 1.f : 0.f;
     }
     for (int qi = tid; qi < nst * kQuadsPerStage; qi += kPotThreads) {
         int d, e0;
@@ -395,39 +401,49 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     const uint32_t tmem = *tmem_slot;
 
     if (warp < 8) {
-        // ======================= A-operand generators and epilogue ============================
+        // ======================= A-operand generators ==========================================
         // No named barriers here: every hand-over is an mbarrier with a bounded wait, and each
         // warp leaves the tile loop as a whole (warp-uniform ok), so a timeout cannot strand a
         // thread at a barrier that the others will never reach.
         const int row_l = tid & (kBM - 1), half = tid >> 7;
         const int g = row_l >> 3, rr = row_l & 7;
-        const float* myq = sq + row_l * NS;
+        // a tile's bead coordinates, copied asynchronously (4-byte cp.async straight into the
+        // row-major slots of buffer tl & 1) one tile ahead of their use; rows past the end are 0
+        auto prefetch = [&](int tl) {
+            float* dst = sq + (tl & 1) * kBM * NS;
+            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
+            for (int i = tid; i < kBM * N; i += kGenThreads) {
+                const int r2 = i % kBM, j = i / kBM;
+                const int64_t row = r0 + r2;
+                float* d = dst + r2 * NS + j;
+                if (row < rows) {
+                    const int64_t x = row / P;
+                    const int p = static_cast<int>(row - x * P);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;"
+                                 ::"r"(smem_u32(d)), "l"(q + (x * N + j) * P + p) : "memory");
+                } else {
+                    *d = 0.f;
+                }
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+        };
         int it = 0;
         bool ok = true;
+        if (my_tiles > 0) prefetch(0);
         for (int tl = 0; tl < my_tiles; ++tl) {
             ok = __all_sync(0xffffffffu, ok && !*err);
             if (!ok) break;
-            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
-            if (tl > 0) ok = mbar_wait_or_err(sq_done, (tl - 1) & 1, err);      // sq of tile tl-1 read
+            // buffer (tl + 1) & 1 is free once every generator has finished tile tl - 1
+            if (tl > 0) ok = mbar_wait_or_err(sq_done, (tl - 1) & 1, err);
+            const bool ahead = ok && tl + 1 < my_tiles;
+            if (ahead) prefetch(tl + 1);
             if (ok) {
-                for (int i = tid; i < kBM * N; i += kGenThreads) {
-                    const int r2 = i % kBM, j = i / kBM;
-                    const int64_t row = r0 + r2;
-                    float v = 0.f;
-                    if (row < rows) {
-                        const int64_t x = row / P;
-                        const int p = static_cast<int>(row - x * P);
-                        v = __ldg(q + (x * N + j) * P + p);
-                    }
-                    sq[r2 * NS + j] = v;
-                }
-                for (int i = tid; i < kBM * (NS - N); i += kGenThreads) {
-                    const int r2 = i / (NS - N), j = N + i % (NS - N);
-                    sq[r2 * NS + j] = (j == q_one(N)) ? 1.f : 0.f;
-                }
+                if (ahead) asm volatile("cp.async.wait_group 1;" ::: "memory");
+                else asm volatile("cp.async.wait_group 0;" ::: "memory");
                 mbar_arrive(sq_ready);
                 ok = mbar_wait_or_err(sq_ready, tl & 1, err);
             }
+            const float* myq = sq + (tl & 1) * kBM * NS + row_l * NS;
             for (int st = 0; st < nst; ++st, ++it) {
                 const int b = it % NB, use = it / NB;
                 if (ok && use > 0) ok = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
@@ -451,15 +467,23 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                 mbar_arrive(full_a + b);
             }
             if (ok) mbar_arrive(sq_done);
-            // epilogue: this warp's 32 rows, every other 16-column chunk
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");          // no copy in flight at exit
+    } else if (warp >= 10) {
+        // ======================= epilogue warpgroup: TMEM -> V =================================
+        const int lg = warp & 3;                                  // TMEM lanes 32 lg .. 32 lg + 31
+        bool ok = true;
+        for (int tl = 0; tl < my_tiles; ++tl) {
+            ok = __all_sync(0xffffffffu, ok && !*err);
+            if (!ok) break;
             const int acc = tl & 1;
-            if (ok) ok = mbar_wait_or_err(acc_full + acc, (tl >> 1) & 1, err);
-            ok = __all_sync(0xffffffffu, ok);       // tcgen05.ld is warp-collective
+            ok = mbar_wait_or_err(acc_full + acc, (tl >> 1) & 1, err);
+            ok = __all_sync(0xffffffffu, ok);                     // tcgen05.ld is warp-collective
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int lg = warp & 3, ch = warp >> 2;
+            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
             const int64_t row = r0 + lg * 32 + lane;
-            for (int c0 = ch * 16; c0 < A2P; c0 += 32) {
+            for (int c0 = 0; c0 < A2P; c0 += 16) {
                 float v[16];
                 tmem_ld16(tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(acc * A2P + c0), v);
                 if (row < rows) {

@@ -48,18 +48,21 @@ __host__ __device__ constexpr int wide_mr(int AP, int K) { return 2 * wide_kp(K)
 // record: [O series (K+1) x AP][rho log terms AP][ln S12] padded to 4
 __host__ __device__ constexpr int wide_rl(int AP, int K) { return ((K + 1) * AP + AP + 1 + 3) / 4 * 4; }
 
+// shared memory (floats): tables | per window: bead records, matrix-exponential buffers and the
+// window's V rows (prefetched with cp.async) -- reused by the chunk-combine slots afterwards
 struct WidePlan {
-    int c, rc, tab, rec, xb, comb, lsum, total_bytes;
-    __host__ __device__ WidePlan(int AP, int K, int N, int G, int W) {
+    int c, rc, tab, rec, xb, vwin, comb, lsum, total_bytes;
+    __host__ __device__ WidePlan(int AP, int K, int N, int G, int W, int ld) {
         int o = 0;
         auto take = [&](int n) { int r = o; o = (o + n + 3) / 4 * 4; return r; };
         c = take((K + 1) * AP);
         rc = take(AP);
         tab = take(N * wide_mr(AP, K));
-        const int recs = G * W * wide_rl(AP, K) + kWideTeams * 2 * AP * AP;
+        const int recs = G * W * wide_rl(AP, K) + kWideTeams * 2 * AP * AP + G * W * ld;
         const int combs = G * ((K + 1) * AP * AP + 4);
         rec = take(recs > combs ? recs : combs);
         xb = rec + G * W * wide_rl(AP, K);
+        vwin = xb + kWideTeams * 2 * AP * AP;
         comb = rec;
         lsum = take(G * (AP + 2) * 2);                         // doubles
         total_bytes = o * 4;
@@ -161,7 +164,20 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
         for (int c = 0; c < AP; ++c) nrow[k][c] = 0.f;
     const int nwin = (C + W - 1) / W;
 
+    float* s_vwin = sm + plan.vwin;
+    const int ld = args.vq_ld;
     for (int w = 0; w < nwin; ++w) {
+        // the window's V rows, copied asynchronously while the records are computed
+        for (int idx = tid; idx < G * W * (ld / 4); idx += kWideThreads) {
+            const int sl = idx / (ld / 4), ch = idx - sl * (ld / 4);
+            const int g = sl / W, lp = w * W + (sl - g * W);
+            const int p = g * C + lp;
+            if (lp < C && p < P)
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                             ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(s_vwin + sl * ld + 4 * ch))),
+                               "l"(vx + static_cast<int64_t>(p) * ld + 4 * ch) : "memory");
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
         // ================================ phase B1: bead records ===============================
         for (int sl0 = 0; sl0 < G * W; sl0 += kWideThreads / 2) {     // uniform trip count
             const int sl = sl0 + (tid >> 1);
@@ -183,6 +199,7 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
             float rdsum = 0.f;
             if (valid) {
                 const int pn = (p + 1 == P) ? 0 : p + 1;
+#pragma unroll 2
                 for (int j = 0; j < N; ++j) {
                     const float* rec = s_tab + j * MR;
                     float cs[KP], th[KP], dv[AH], rdv[AH], rx[4];
@@ -243,6 +260,7 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
                 }
             }
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
 
         // ================================ phase B2: exp(-tau V), ring product ==================
@@ -253,12 +271,12 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
                 if (lp >= C || p >= pe) break;                 // team-uniform
                 // V row r (symmetric, packed pairs), padded with zeros
                 float b[AP];
-                const float* vr = vx + static_cast<int64_t>(p) * args.vq_ld;
+                const float* vr = s_vwin + (team * W + i) * ld;
                 float dg = 0.f;
 #pragma unroll
                 for (int c = 0; c < AP; ++c) {
                     const int hi = r > c ? r : c, lo = r > c ? c : r;
-                    b[c] = (r < A && c < A) ? __ldg(vr + hi * (hi + 1) / 2 + lo) : 0.f;
+                    b[c] = (r < A && c < A) ? vr[hi * (hi + 1) / 2 + lo] : 0.f;
                     if (c == r) dg = b[c];
                 }
                 const float vmean = team_sum(dg, tmask) / float(A);
@@ -274,22 +292,34 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
                 const float sc = ldexpf(1.f, -s);
 #pragma unroll
                 for (int c = 0; c < AP; ++c) b[c] *= sc;
-                // Horner: X = I + B X / k for k = m .. 1, starting from X = I
-                float xr[AP];
-#pragma unroll
-                for (int c = 0; c < AP; ++c) xr[c] = (c == r ? 1.f : 0.f) + b[c] * (1.f / float(kWideTaylor));
-                float* cur = xb0;
-                float* nxt = xb1;
-                for (int k = kWideTaylor - 1; k >= 1; --k) {
-                    if (r < AP) stv(cur + r * AP, xr);
-                    __syncwarp(tmask);
+                // Taylor polynomial of degree 8, Paterson-Stockmeyer: with C_i = c_3i I + c_3i+1 B +
+                // c_3i+2 B^2 (c_k = 1/k!), exp(B) ~ C_0 + B^3 (C_1 + B^3 C_2): four matrix products
+                float* x0 = xb0;
+                float* x1 = xb1;
+                if (r < AP) stv(x0 + r * AP, b);
+                __syncwarp(tmask);
+                float b2[AP], xr[AP];
+                row_times<AP>(b, x0, b2);
+                row_times<AP>(b2, x0, xr);                      // row of B^3
+                if (r < AP) stv(x1 + r * AP, xr);
+                __syncwarp(tmask);
+                constexpr float c3 = 1.f / 6.f, c4 = 1.f / 24.f, c5 = 1.f / 120.f, c6 = 1.f / 720.f,
+                                c7 = 1.f / 5040.f, c8 = 1.f / 40320.f;
+                {
                     float t[AP];
-                    row_times<AP>(b, cur, t);
-                    const float inv = 1.f / float(k);
 #pragma unroll
-                    for (int c = 0; c < AP; ++c) xr[c] = (c == r ? 1.f : 0.f) + t[c] * inv;
-                    float* tmp = cur; cur = nxt; nxt = tmp;
+                    for (int c = 0; c < AP; ++c) t[c] = (c == r ? c6 : 0.f) + c7 * b[c] + c8 * b2[c];
+                    row_times<AP>(t, x1, xr);                   // C_2 B^3
+#pragma unroll
+                    for (int c = 0; c < AP; ++c) t[c] = (c == r ? c3 : 0.f) + c4 * b[c] + c5 * b2[c] + xr[c];
+                    row_times<AP>(t, x1, xr);                   // (C_1 + C_2 B^3) B^3
+#pragma unroll
+                    for (int c = 0; c < AP; ++c) xr[c] += (c == r ? 1.f : 0.f) + b[c] + 0.5f * b2[c];
                 }
+                // squarings; x0 / x1 alternate (every row of the buffer read is complete before
+                // it is replaced: a warp barrier separates each write from the reads before it)
+                float* cur = x0;
+                float* nxt = x1;
                 for (int sq = 0; sq < s; ++sq) {
                     if (r < AP) stv(cur + r * AP, xr);
                     __syncwarp(tmask);
@@ -475,10 +505,10 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
 }
 
 template <int AP, int K>
-__global__ void __launch_bounds__(kWideThreads, 1) pimc_wide_kernel(const WideArgs args) {
+__global__ void __launch_bounds__(kWideThreads, AP <= 12 ? 2 : 1) pimc_wide_kernel(const WideArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);
-    const WidePlan plan(AP, K, args.m.N, args.G, args.W);
+    const WidePlan plan(AP, K, args.m.N, args.G, args.W, args.vq_ld);
     wide_load_tables<AP, K>(args.m, sm, plan);
     __syncthreads();
     for (int64_t x = blockIdx.x; x < args.X; x += gridDim.x) wide_sample<AP, K>(args, sm, plan, x);
@@ -487,7 +517,7 @@ __global__ void __launch_bounds__(kWideThreads, 1) pimc_wide_kernel(const WideAr
 // Host launcher (one instantiation per padded width AP and series order K).
 template <int AP, int K>
 int launch_wide_one(const WideArgs& args, cudaStream_t stream) {
-    const WidePlan plan(AP, K, args.m.N, args.G, args.W);
+    const WidePlan plan(AP, K, args.m.N, args.G, args.W, args.vq_ld);
     auto kern = pimc_wide_kernel<AP, K>;
     if (plan.total_bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
     static int configured = 0;

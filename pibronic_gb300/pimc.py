@@ -504,6 +504,8 @@ def evaluate_device(plan, X, seed=None, offset=0, q=None, plus_minus=True, want_
         setattr(o, name, out[key].data_ptr() if key in out else None)
     o.status = status.data_ptr()
     sh = _native.stream_handle(stream)
+    if q is not None and q.dtype == torch.float64 and getattr(plan, "use_tc", False):
+        q = q.float()          # the tensor-core form evaluates FP32 bead coordinates
     if q is None and getattr(plan, "use_tc", False):
         scratch = plan.tc_scratch()
         rc = lib.pbr_sample_eval_tc(plan.struct, int(seed), int(offset), int(X), o, scratch.data_ptr(),
@@ -512,6 +514,9 @@ def evaluate_device(plan, X, seed=None, offset=0, q=None, plus_minus=True, want_
         rc = lib.pbr_sample_eval(plan.struct, int(seed), int(offset), int(X), o, sh)
     elif q.dtype == torch.float64:
         rc = lib.pbr_eval_q(plan.struct, _native.ptr(q), int(X), o, sh)
+    elif getattr(plan, "use_tc", False):
+        scratch = plan.tc_scratch()
+        rc = lib.pbr_eval_q_tc(plan.struct, _native.ptr(q), int(X), o, scratch.data_ptr(), scratch.numel(), sh)
     else:
         rc = lib.pbr_eval_q_f32(plan.struct, _native.ptr(q), int(X), o, sh)
     _native.check(rc, "fused block evaluation")
