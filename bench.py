@@ -530,7 +530,7 @@ def large_leg(args):
     _native.check(lib.pbr_tc_potential_dims(N, A, ctypes.byref(n2p), ctypes.byref(a2p)), "dims")
     n2p, a2p = n2p.value, a2p.value
     Xc = min(X, max(1, (64 << 20) // (4 * P * (N + a2p))))
-    bp = torch.empty(2 * a2p * n2p, dtype=torch.float32, device="cuda")
+    bp = torch.empty(int(lib.pbr_tc_potential_packed_floats(N, A)), dtype=torch.float32, device="cuda")
     vq = torch.empty((Xc * P, a2p), dtype=torch.float32, device="cuda")
     t_ = plan.tensors
     sh = _native.stream_handle()
@@ -548,9 +548,12 @@ def large_leg(args):
         if i:
             ts.append(e0.elapsed_time(e1) * 1e-3)
     t_tc = min(ts)
-    issued = 6.0 * Xc * P * a2p * n2p / t_tc / 1e12
+    mp = int(lib.pbr_tc_potential_packed_floats(N, A)) // (2 * n2p)     # pair columns incl. padding
+    issued = 6.0 * Xc * P * mp * n2p / t_tc / 1e12
     useful = 2.0 * Xc * P * (A * (A + 1) // 2) * (N * (N + 1) // 2 + N + 1) / t_tc / 1e12
     peak = tf32_cublas_peak(torch)
+    rate, cyc = ctypes.c_double(), ctypes.c_double()
+    _native.check(lib.pbr_tc_mma_rate(128, 256, 4096, ctypes.byref(rate), ctypes.byref(cyc), sh), "mma rate")
 
     def summary(e, t):
         rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
@@ -564,7 +567,10 @@ def large_leg(args):
            "plain": summary(ep, tp),
            "tc_gemm": {"chunk_samples": Xc, "ms": 1e3 * t_tc, "issued_tflops": issued, "useful_tflops": useful,
                        "tf32_cublas_tflops_measured": peak, "frac_of_measured_tf32": issued / peak,
-                       "note": "issued = 3 TF32 passes (hi/lo split) x padded K and columns"}}
+                       "tf32_mma_128x256x8_tflops_measured": rate.value,
+                       "cycles_per_mma_measured": cyc.value,
+                       "frac_of_measured_mma_rate": issued / rate.value,
+                       "note": "issued = 3 TF32 passes (hi/lo split) x padded K x padded pair columns"}}
     if not args.no_learned:
         fl = FlowProposal(data.prepared, plan, nsel=2, layers=8, hidden=128, seed=0)
         y, _ = fl.prepare(plain["q"])

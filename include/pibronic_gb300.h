@@ -381,13 +381,21 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
  * pbr_tc_potential_dims gives the padded K extent n2p and the column count a2p (A(A+1)/2 rounded up
  * to 16).  pbr_tc_pack_potential turns vib_qq [N(N+1)/2][A(A+1)/2], vib_l [N][A(A+1)/2] and vib_e
  * [A(A+1)/2] (FP32 or FP64 as precision says; vib_l and vib_e nullable = zero) into b_packed
- * (2 * a2p * n2p floats, 16-byte aligned): per stage of 32 K columns, the TF32 hi part then the lo
- * part, each a2p rows x 8 cores of 4 columns, core (row r, core c) at ((r/8)*8 + c)*8 + r%8 in
- * 16-byte units.  pbr_tc_potential writes vq [X * P][a2p] (FP32; row sample * P + bead, column
- * pair_index(b, c)) from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in
- * pbr_tc_gemm.  Replaces pimc.py:1145-1150 (V of diagonalize_coupling_matrix).
+ * (pbr_tc_potential_packed_floats(N, A) = 2 * a2p * n2p floats, 16-byte aligned): per stage of 32
+ * K columns, the TF32 hi part then the lo part, each a2p rows x 8 cores of 4 columns, core (row r,
+ * core c) at ((r/8)*8 + c)*8 + r%8 in 16-byte units.
+ * pbr_tc_potential writes vq [X * P][a2p] (FP32; row sample * P + bead, column pair_index(b, c))
+ * from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in pbr_tc_gemm.  Replaces
+ * pimc.py:1145-1150 (V of diagonalize_coupling_matrix).
  */
+/* Tensor-pipe rate: one CTA per SM issues reps back-to-back tcgen05.mma kind::tf32 (M x N x 8,
+ * M 64 or 128, 16 <= N <= 256) from one thread; *tflops is the whole-GPU rate, *cycles_per_mma the
+ * issuing thread's cycles per instruction.  Allocates and frees two small device buffers (a
+ * measurement, not a path entry point).  No counterpart in the reference. */
+int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, double* tflops, double* cycles_per_mma, void* stream);
+
 int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
+int64_t pbr_tc_potential_packed_floats(int32_t N, int32_t A);
 int pbr_tc_pack_potential(const void* vib_qq, const void* vib_l, const void* vib_e, int32_t precision,
                           int32_t N, int32_t A, void* b_packed, void* stream);
 int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const void* b_packed,

@@ -33,7 +33,8 @@ EXPORTED = (
     "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
     "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
     "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
-    "pbr_tc_gemm", "pbr_tc_potential_dims", "pbr_tc_pack_potential", "pbr_tc_potential",
+    "pbr_tc_gemm", "pbr_tc_mma_rate", "pbr_tc_potential_dims", "pbr_tc_potential_packed_floats", "pbr_tc_pack_potential",
+    "pbr_tc_potential",
     "pbr_sample_eval_tc_scratch", "pbr_sample_eval_tc", "pbr_eval_q_tc", "pbr_version",
 )
 
@@ -119,6 +120,8 @@ def _declare(lib):
         "pbr_reduce_segments_scratch": (i64, [i32]),
         "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
+        "pbr_tc_potential_packed_floats": (i64, [i32, i32]),
+        "pbr_tc_mma_rate": (C.c_int, [i32, i32, i32, C.POINTER(f64), C.POINTER(f64), vp]),
         "pbr_tc_pack_potential": (C.c_int, [vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp]),
         "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),

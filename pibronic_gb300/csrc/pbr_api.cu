@@ -11,6 +11,7 @@ template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
 template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, cudaStream_t);
 int tc_quadratic_cols(int A);
 int tc_quadratic_kdim(int N);
+int64_t tc_packed_floats(int N, int A);
 int tc_quadratic_launch(const float*, int64_t, int, int, int, const void*, float*, int32_t*, cudaStream_t);
 int tc_pack_launch(const void*, const void*, const void*, int, int, int, void*, cudaStream_t);
 extern template int launch_wide<12>(int, const WideArgs&, cudaStream_t);   // pbr_wide_a12.cu
@@ -355,8 +356,7 @@ constexpr int64_t kScratchAlign = 256;
 int64_t align_bytes(int64_t n) { return (n + kScratchAlign - 1) / kScratchAlign * kScratchAlign; }
 
 int64_t tc_fixed_bytes(const pbr_model& m) {
-    const int64_t b = static_cast<int64_t>(pbr::tc_quadratic_cols(m.A)) * pbr::tc_quadratic_kdim(m.N) * 4;
-    return align_bytes(2 * b) + kScratchAlign;
+    return align_bytes(pbr::tc_packed_floats(m.N, m.A) * 4) + kScratchAlign;
 }
 
 // The wide form's tile: up to 16 teams per sample, windows of up to 8 beads per team.

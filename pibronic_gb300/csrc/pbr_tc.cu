@@ -246,16 +246,11 @@ constexpr int kEpiThreads = 128;                      // warps 10-13
 constexpr int kPotThreads = kGenThreads + 64 + kEpiThreads;   // + MMA warp, B-loader warp, epilogue
 constexpr int kQStageK = 32;                          // TF32 elements of K per stage (128 B)
 constexpr int kQuadsPerStage = kQStageK / 4;
-constexpr int kAStage = kBM * kStageBytesK;           // one 128-row operand part of one stage
+constexpr int kAStageCols = 2 * kQStageK;             // TMEM columns of one A stage (hi, lo)
 
-// slot of the constant 1 (16-byte aligned), and the row stride of the slots in shared memory:
-// >= NA + 4 and == 4 (mod 8) for conflict-free 128-bit loads by consecutive rows
+// slot of the constant 1, and the number of slots per bead row (q, zeros, 1, 0, 0, 0)
 __host__ __device__ inline int q_one(int N) { return (N + 3) / 4 * 4; }
-__host__ __device__ inline int q_stride(int N) {
-    int ns = q_one(N) + 4;
-    if (ns % 8 == 0) ns += 4;
-    return ns;
-}
+__host__ __device__ inline int q_slots(int N) { return q_one(N) + 4; }
 
 // number of quads before padding, and quad qi -> (d, e0)
 __host__ __device__ inline int quad_count(int N) {
@@ -275,19 +270,28 @@ __host__ __device__ inline void quad_of(int qi, int N, int& d, int& e0) {
     d = na + 1; e0 = na;                                // padding: 0 * [1, 0, 0, 0]
 }
 
+// shared memory: B stages, two tiles of bead coordinates (mode-major: slot j of row r at
+// j * 128 + r, so consecutive rows read consecutive words), the quad table, barriers.  The A
+// operand never goes through shared memory: the generators store it into TMEM.
 struct PotSmem {
-    int nb, a, b, q, quads, bars, total;
+    int nb, b, q, quads, bars, total;
     __host__ __device__ PotSmem(int N, int A2P, int nst, int nbuf) {
         nb = nbuf;
         int o = 0;
-        a = o;     o += nb * 2 * kAStage;                           // [buffer][hi, lo]
         b = o;     o += nb * 2 * A2P * kStageBytesK;                // [buffer][hi, lo]
-        q = o;     o += 2 * kBM * q_stride(N) * 4;                  // two tiles of bead coordinates
+        q = o;     o += 2 * kBM * q_slots(N) * 4;                   // two tiles
         quads = o; o += ((nst * kQuadsPerStage * 4 + 15) / 16) * 16;
         bars = o;  o += (3 * nb + 6) * 8 + 16;                      // barriers, TMEM slot, error flag
         total = o;
     }
 };
+
+// TMEM columns: two accumulators (2 x A2P), then nb A stages of 64 columns (hi 32, lo 32)
+__host__ __device__ inline int pot_tmem_cols(int A2P, int nb) {
+    int c = 32;
+    while (c < 2 * A2P + nb * kAStageCols) c <<= 1;
+    return c;
+}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar))
@@ -320,6 +324,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 __device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
+// 16 consecutive 32-bit TMEM columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+          "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+          "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+          "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+          "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+
+// D (TMEM) += A (TMEM, K-major: lane = row, 32-bit column = k) x B (shared memory descriptor)
+__device__ __forceinline__ void mma_tf32_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -348,7 +375,6 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     extern __shared__ __align__(1024) unsigned char tsm[];
     const PotSmem L(N, A2P, nst, nbuf);
     const int NB = L.nb;
-    unsigned char* sa = tsm + L.a;
     unsigned char* sb = tsm + L.b;
     float* sq = reinterpret_cast<float*>(tsm + L.q);
     uint32_t* squad = reinterpret_cast<uint32_t*>(tsm + L.quads);
@@ -361,7 +387,7 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     uint64_t* sq_done = sq_ready + 1;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sq_done + 1);
     volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
-    const int NS = q_stride(N);
+    const int NSL = q_slots(N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t BSTAGE = static_cast<uint32_t>(A2P) * kStageBytesK;
     const int64_t rows = X * P;
@@ -385,9 +411,10 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         mbar_init(sq_done, kGenThreads);
         *err = 0;
     }
-    for (int i = tid; i < 2 * kBM * (NS - N); i += kPotThreads) {      // the constant slots of both tiles
-        const int r2 = i / (NS - N), j = N + i % (NS - N);
-        sq[r2 * NS + j] = (j == q_one(N)) ? 1.f : 0.f;
+    for (int i = tid; i < 2 * kBM * (NSL - N); i += kPotThreads) {     // the constant slots of both tiles
+        const int t = i / (kBM * (NSL - N)), rem = i - t * kBM * (NSL - N);
+        const int j = N + rem / kBM, r2 = rem % kBM;
+        sq[t * kBM * NSL + j * kBM + r2] = (j == q_one(N)) ? 1.f : 0.f;
     }
     for (int qi = tid; qi < nst * kQuadsPerStage; qi += kPotThreads) {
         int d, e0;
@@ -406,16 +433,16 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         // warp leaves the tile loop as a whole (warp-uniform ok), so a timeout cannot strand a
         // thread at a barrier that the others will never reach.
         const int row_l = tid & (kBM - 1), half = tid >> 7;
-        const int g = row_l >> 3, rr = row_l & 7;
+        const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;   // this warp's TMEM lanes
         // a tile's bead coordinates, copied asynchronously (4-byte cp.async straight into the
-        // row-major slots of buffer tl & 1) one tile ahead of their use; rows past the end are 0
+        // mode-major slots of buffer tl & 1) one tile ahead of their use; rows past the end are 0
         auto prefetch = [&](int tl) {
-            float* dst = sq + (tl & 1) * kBM * NS;
+            float* dst = sq + (tl & 1) * kBM * NSL;
             const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
             for (int i = tid; i < kBM * N; i += kGenThreads) {
                 const int r2 = i % kBM, j = i / kBM;
                 const int64_t row = r0 + r2;
-                float* d = dst + r2 * NS + j;
+                float* d = dst + j * kBM + r2;
                 if (row < rows) {
                     const int64_t x = row / P;
                     const int p = static_cast<int>(row - x * P);
@@ -443,27 +470,31 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                 mbar_arrive(sq_ready);
                 ok = mbar_wait_or_err(sq_ready, tl & 1, err);
             }
-            const float* myq = sq + (tl & 1) * kBM * NS + row_l * NS;
+            const float* myq = sq + (tl & 1) * kBM * NSL + row_l;
             for (int st = 0; st < nst; ++st, ++it) {
                 const int b = it % NB, use = it / NB;
                 if (ok && use > 0) ok = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
                 if (!ok) continue;
-                unsigned char* ahi = sa + b * 2 * kAStage;
-                unsigned char* alo = ahi + kAStage;
+                // this thread's row, K columns half * 16 .. half * 16 + 15 of the stage
+                float hi[16], lo[16];
 #pragma unroll
                 for (int u = 0; u < kQuadsPerStage / 2; ++u) {
-                    const int c = half * (kQuadsPerStage / 2) + u;          // 16-byte core column
-                    const uint32_t de = squad[st * kQuadsPerStage + c];
-                    const float qd = myq[de & 0xFFFFu];
-                    const float4 qe = *reinterpret_cast<const float4*>(myq + (de >> 16));
-                    const float x0 = qd * qe.x, x1 = qd * qe.y, x2 = qd * qe.z, x3 = qd * qe.w;
-                    const float h0 = tf32_trunc(x0), h1 = tf32_trunc(x1), h2 = tf32_trunc(x2), h3 = tf32_trunc(x3);
-                    const int off = ((g * (kStageBytesK / 16) + c) * 8 + rr) * 16;
-                    *reinterpret_cast<float4*>(ahi + off) = make_float4(h0, h1, h2, h3);
-                    *reinterpret_cast<float4*>(alo + off) = make_float4(tf32_trunc(x0 - h0), tf32_trunc(x1 - h1),
-                                                                        tf32_trunc(x2 - h2), tf32_trunc(x3 - h3));
+                    const uint32_t de = squad[st * kQuadsPerStage + half * (kQuadsPerStage / 2) + u];
+                    const int d = static_cast<int>(de & 0xFFFFu), e0 = static_cast<int>(de >> 16);
+                    const float qd = myq[d * kBM];
+#pragma unroll
+                    for (int v = 0; v < 4; ++v) {
+                        const float x = qd * myq[(e0 + v) * kBM];
+                        const float h = tf32_trunc(x);
+                        hi[4 * u + v] = h;
+                        lo[4 * u + v] = x - h;           // the tensor core reads its TF32 bits
+                    }
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const uint32_t col = static_cast<uint32_t>(2 * A2P + b * kAStageCols + half * 16);
+                tmem_st16(tmem + lane_base + col, hi);
+                tmem_st16(tmem + lane_base + col + kQStageK, lo);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 mbar_arrive(full_a + b);
             }
             if (ok) mbar_arrive(sq_done);
@@ -518,20 +549,18 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const unsigned char* ahi = sa + b * 2 * kAStage;
-                    const unsigned char* alo = ahi + kAStage;
+                    const uint32_t ahi = tmem + static_cast<uint32_t>(2 * A2P + b * kAStageCols);
+                    const uint32_t alo = ahi + kQStageK;
                     const unsigned char* bhi = sb + (resident ? st : b) * 2 * BSTAGE;
                     const unsigned char* blo = bhi + BSTAGE;
 #pragma unroll
                     for (int kk = 0; kk < kQStageK; kk += 8) {
                         const uint32_t off = static_cast<uint32_t>(kk * 4 / 16) * 128;
-                        const uint64_t dah = smem_desc(smem_u32(ahi) + off, LBO, SBO);
-                        const uint64_t dal = smem_desc(smem_u32(alo) + off, LBO, SBO);
                         const uint64_t dbh = smem_desc(smem_u32(bhi) + off, LBO, SBO);
                         const uint64_t dbl = smem_desc(smem_u32(blo) + off, LBO, SBO);
-                        mma_issue<2>(dtm, dah, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
-                        mma_issue<2>(dtm, dah, dbl, idesc, 1u);
-                        mma_issue<2>(dtm, dal, dbh, idesc, 1u);
+                        mma_tf32_ts(dtm, ahi + kk, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32_ts(dtm, ahi + kk, dbl, idesc, 1u);
+                        mma_tf32_ts(dtm, alo + kk, dbh, idesc, 1u);
                     }
                     mma_commit(empty + b);
                     last = empty + b;
@@ -616,9 +645,11 @@ __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ l
     }
 }
 
+// stage buffers: as many as 4 that fit both the shared memory (B stages) and the TMEM (A stages
+// beside the two accumulators)
 int pot_buffers(int N, int A2P, int nst) {
-    for (int nb = 3; nb >= 2; --nb)
-        if (PotSmem(N, A2P, nst, nb).total <= 227 * 1024) return nb;
+    for (int nb = 4; nb >= 2; --nb)
+        if (PotSmem(N, A2P, nst, nb).total <= 227 * 1024 && 2 * A2P + nb * kAStageCols <= 512) return nb;
     return 0;
 }
 
@@ -628,6 +659,7 @@ namespace pbr {
 
 int tc_quadratic_cols(int A) { return (A * (A + 1) / 2 + 15) / 16 * 16; }
 int tc_quadratic_kdim(int N) { return (quad_count(N) + kQuadsPerStage - 1) / kQuadsPerStage * kQStageK; }
+int64_t tc_packed_floats(int N, int A) { return static_cast<int64_t>(2) * tc_quadratic_cols(A) * tc_quadratic_kdim(N); }
 
 int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const void* bpack, float* vq,
                         int32_t* status, cudaStream_t stream) {
@@ -636,10 +668,9 @@ int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const 
     if ((reinterpret_cast<uintptr_t>(bpack) | reinterpret_cast<uintptr_t>(vq)) & 15) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int nst = tc_quadratic_kdim(N) / kQStageK;
-    int ncols = 32;
-    while (ncols < 2 * A2P) ncols <<= 1;
     const int nb = pot_buffers(N, A2P, nst);
     if (nb == 0) return PBR_ERR_UNSUPPORTED;
+    const int ncols = pot_tmem_cols(A2P, nb);
     const PotSmem L(N, A2P, nst, nb);
     static int configured = 0;
     if (L.total > configured) {
@@ -691,6 +722,11 @@ int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p) {
     return PBR_OK;
 }
 
+int64_t pbr_tc_potential_packed_floats(int32_t N, int32_t A) {
+    if (N < 1 || N > 64 || A < 1 || A > 16) return -1;
+    return pbr::tc_packed_floats(N, A);
+}
+
 int pbr_tc_pack_potential(const void* vib_qq, const void* vib_l, const void* vib_e, int32_t precision, int32_t N,
                           int32_t A, void* b_packed, void* stream) {
     return pbr::tc_pack_launch(vib_qq, vib_l, vib_e, precision, N, A, b_packed, static_cast<cudaStream_t>(stream));
@@ -704,3 +740,95 @@ int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Tensor-pipe rate probe: each CTA (one per SM) issues `reps` back-to-back tcgen05.mma kind::tf32
+// (M x N x 8, operands zeros in shared memory, one TMEM accumulator) from one thread, commits once
+// and waits (bounded).  Reports the issuing thread's cycles per MMA and the whole-GPU TF/s; the
+// denominator the potential GEMM is held against.
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+__global__ void tc_rate_kernel(int M, int N, int reps, int32_t* flag, long long* cycles) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char* sa = sm;                 // 128 rows x 32 B (K = 8 tf32)
+    unsigned char* sb = sm + 128 * 32;      // 256 rows x 32 B
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 128 * 32 + 256 * 32);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+    for (int i = threadIdx.x; i < (128 + 256) * 32 / 4; i += blockDim.x) reinterpret_cast<float*>(sm)[i] = 0.f;
+    int ncols = 32;
+    while (ncols < N) ncols <<= 1;
+    if (threadIdx.x < 32) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                     "r"(ncols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) mbar_init(bar, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = *slot;
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = instr_desc(2, M, N);
+        const uint64_t da = smem_desc(smem_u32(sa), 128, 256), db = smem_desc(smem_u32(sb), 128, 256);
+        const long long t0 = clock64();
+        for (int i = 0; i < reps; ++i) mma_issue<2>(tmem, da, db, idesc, i > 0 ? 1u : 0u);
+        mma_commit(bar);
+        const bool done = mbar_wait(bar, 0);
+        const long long t1 = clock64();
+        if (!done) atomicExch(flag, 1);
+        if (blockIdx.x == 0) *cycles = t1 - t0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (threadIdx.x < 32)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+}  // namespace
+
+extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, double* tflops, double* cycles_per_mma,
+                               void* stream) {
+    if ((M != 64 && M != 128) || N < 16 || N > 256 || N % 16 != 0 || reps < 1 || reps > (1 << 20) || !tflops ||
+        !cycles_per_mma)
+        return PBR_ERR_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int dev = 0, sms = 0;
+    PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
+    PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    constexpr int kSmem = 120 * 1024;      // one CTA per SM
+    if (cudaFuncSetAttribute(tc_rate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem) != cudaSuccess)
+        return PBR_ERR_UNSUPPORTED;
+    int32_t* dflag = nullptr;
+    long long* dcyc = nullptr;
+    PBR_CUDA_CHECK_RET(cudaMalloc(&dflag, sizeof(int32_t)));
+    PBR_CUDA_CHECK_RET(cudaMalloc(&dcyc, sizeof(long long)));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = PBR_OK;
+    cudaMemsetAsync(dflag, 0, sizeof(int32_t), st);
+    tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, 64, dflag, dcyc);        // warm-up
+    cudaEventRecord(e0, st);
+    tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, reps, dflag, dcyc);
+    cudaEventRecord(e1, st);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = PBR_ERR_CUDA;
+    float ms = 0.f;
+    long long cyc = 0;
+    int32_t flag = 0;
+    if (rc == PBR_OK) {
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaMemcpy(&cyc, dcyc, sizeof(cyc), cudaMemcpyDeviceToHost);
+        cudaMemcpy(&flag, dflag, sizeof(flag), cudaMemcpyDeviceToHost);
+        if (flag) rc = PBR_ERR_CUDA;
+    }
+    *tflops = (ms > 0.f) ? 2.0 * M * N * 8.0 * reps * sms / (ms * 1e-3) / 1e12 : 0.0;
+    *cycles_per_mma = static_cast<double>(cyc) / reps;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(dflag);
+    cudaFree(dcyc);
+    return rc;
+}

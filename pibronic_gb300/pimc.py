@@ -504,21 +504,28 @@ def evaluate_device(plan, X, seed=None, offset=0, q=None, plus_minus=True, want_
         setattr(o, name, out[key].data_ptr() if key in out else None)
     o.status = status.data_ptr()
     sh = _native.stream_handle(stream)
-    if q is not None and q.dtype == torch.float64 and getattr(plan, "use_tc", False):
-        q = q.float()          # the tensor-core form evaluates FP32 bead coordinates
-    if q is None and getattr(plan, "use_tc", False):
-        scratch = plan.tc_scratch()
-        rc = lib.pbr_sample_eval_tc(plan.struct, int(seed), int(offset), int(X), o, scratch.data_ptr(),
-                                    scratch.numel(), sh)
-    elif q is None:
-        rc = lib.pbr_sample_eval(plan.struct, int(seed), int(offset), int(X), o, sh)
-    elif q.dtype == torch.float64:
-        rc = lib.pbr_eval_q(plan.struct, _native.ptr(q), int(X), o, sh)
-    elif getattr(plan, "use_tc", False):
-        scratch = plan.tc_scratch()
-        rc = lib.pbr_eval_q_tc(plan.struct, _native.ptr(q), int(X), o, scratch.data_ptr(), scratch.numel(), sh)
-    else:
-        rc = lib.pbr_eval_q_f32(plan.struct, _native.ptr(q), int(X), o, sh)
+    def launch(use_tc):
+        qq = q.float() if (use_tc and q is not None and q.dtype == torch.float64) else q
+        if qq is None and use_tc:
+            scratch = plan.tc_scratch()
+            return lib.pbr_sample_eval_tc(plan.struct, int(seed), int(offset), int(X), o, scratch.data_ptr(),
+                                          scratch.numel(), sh)
+        if qq is None:
+            return lib.pbr_sample_eval(plan.struct, int(seed), int(offset), int(X), o, sh)
+        if qq.dtype == torch.float64:
+            return lib.pbr_eval_q(plan.struct, _native.ptr(qq), int(X), o, sh)
+        if use_tc:
+            scratch = plan.tc_scratch()
+            return lib.pbr_eval_q_tc(plan.struct, _native.ptr(qq), int(X), o, scratch.data_ptr(), scratch.numel(), sh)
+        return lib.pbr_eval_q_f32(plan.struct, _native.ptr(qq), int(X), o, sh)
+
+    use_tc = getattr(plan, "use_tc", False)
+    rc = launch(use_tc)
+    if (rc == _native.PBR_ERR_UNSUPPORTED and not use_tc and plan.precision == 32
+            and plan.variant == plan.VARIANT_AUTO):
+        # a shape the shared-memory forms cannot hold: the tensor-core form from now on
+        plan.use_tc = True
+        rc = launch(True)
     _native.check(rc, "fused block evaluation")
     out["status"] = status
     return out

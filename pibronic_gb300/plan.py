@@ -240,9 +240,14 @@ class DevicePlan:
     #: (pbr_sample_eval_tc, precision 32); 0 lets the library choose
     VARIANT_AUTO, VARIANT_CHUNK, VARIANT_TEAM, VARIANT_TC = 0, 1, 2, 3
 
-    #: auto choice of the tensor-core form: when the quadratic coupling table of the fused forms
-    #: (npair(N) x align4(npair(A)) FP32 values, held in shared memory) exceeds this many bytes
+    #: auto choice of the tensor-core form (measured on GB300, samples/s of both forms): from 5
+    #: surfaces on, when the quadratic coupling table of the shared-memory forms (npair(N) x
+    #: align4(npair(A)) FP32 values) exceeds this many bytes; always beyond 8 surfaces; and for
+    #: any shape the shared-memory forms cannot hold (evaluate_device retries on the tensor-core
+    #: form when they report unsupported sizes).  Up to 4 surfaces the row-team / chunk forms win
+    #: at every N <= 64.
     TC_TABLE_BYTES = 64 * 1024
+    TC_MIN_A = 5
     #: q and V bytes per chunk of the tensor-core form (L2-resident between its launches)
     TC_CHUNK_BYTES = 64 << 20
 
@@ -271,7 +276,7 @@ class DevicePlan:
         self.variant = variant
         n2, a2p = prep.N * (prep.N + 1) // 2, (prep.A * (prep.A + 1) // 2 + 3) // 4 * 4
         self.use_tc = precision == 32 and (variant == self.VARIANT_TC or prep.A > 8 or (
-            variant == self.VARIANT_AUTO and n2 * a2p * 4 > self.TC_TABLE_BYTES))
+            variant == self.VARIANT_AUTO and prep.A >= self.TC_MIN_A and n2 * a2p * 4 > self.TC_TABLE_BYTES))
         self._tc_scratch = None
 
     def tc_scratch(self):

@@ -60,16 +60,16 @@ def _expected_operands(N, A2, qq, lin, en, q_rows):
     return a, B
 
 
-def _unpack(bp, a2p, n2p):
-    """b_packed (stage-major, hi then lo, core layout) -> hi, lo [a2p][n2p]."""
+def _unpack(bp, mp, n2p):
+    """b_packed (stages of 32 K columns, hi then lo, mp rows each, core layout) -> hi, lo [mp][n2p]."""
     nst = n2p // 32
-    hi, lo = np.zeros((a2p, n2p)), np.zeros((a2p, n2p))
-    r = np.arange(a2p)[:, None]
+    hi, lo = np.zeros((mp, n2p)), np.zeros((mp, n2p))
+    r = np.arange(mp)[:, None]
     c = np.arange(8)[None, :]
     for st in range(nst):
-        base = st * 2 * a2p * 32
+        base = st * 2 * mp * 32
         for part, dst in ((0, hi), (1, lo)):
-            blk = bp[base + part * a2p * 32: base + (part + 1) * a2p * 32]
+            blk = bp[base + part * mp * 32: base + (part + 1) * mp * 32]
             for u in range(4):
                 idx = (((r // 8) * 8 + c) * 8 + r % 8) * 4 + u
                 dst[:, st * 32 + c[0] * 4 + u] = blk[idx]
@@ -95,7 +95,10 @@ def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
     dev = {k: (torch.as_tensor(v, dtype=dt).cuda().contiguous() if v is not None else None)
            for k, v in (("qq", qq), ("l", lin), ("e", en))}
     t_q = torch.as_tensor(q).cuda().contiguous()
-    bp = torch.full((2 * a2p * n2p,), float("nan"), dtype=torch.float32, device="cuda")
+    nbp = int(lib.pbr_tc_potential_packed_floats(N, A))
+    mp = nbp // (2 * n2p)
+    assert mp == a2p
+    bp = torch.full((nbp,), float("nan"), dtype=torch.float32, device="cuda")
     vq = torch.full((X * P, a2p), float("nan"), dtype=torch.float32, device="cuda")
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
     sh = _native.stream_handle()
@@ -109,7 +112,7 @@ def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
     a_op, B = _expected_operands(N, A2, qq, lin, en, rows)
     assert B.shape[1] == n2p
     # packed operands: hi + lo reproduce the FP32 couplings in the documented layout, padding zero
-    hi, lo = _unpack(bp.double().cpu().numpy(), a2p, n2p)
+    hi, lo = _unpack(bp.double().cpu().numpy(), mp, n2p)
     assert np.allclose((hi + lo)[:A2], B.astype(np.float32), rtol=5e-7, atol=0)
     assert not (hi + lo)[A2:].any()
     ref = a_op @ B.T
