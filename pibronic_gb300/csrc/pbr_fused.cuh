@@ -186,6 +186,83 @@ __device__ __forceinline__ void jacobi_accumulate(T (&a)[A][A], T (&u)[A][A], in
     }
 }
 
+// exp(-tau V) for a small symmetric V held in registers (FP32): V is shifted by its mean
+// eigenvalue (trace / A), scaled by 2^-s until ||tau (V - mean)||_inf <= 1/2, exponentiated by the
+// degree-8 Taylor polynomial (Paterson-Stockmeyer: C_0 + B^3 (C_1 + B^3 C_2), truncation < 1e-8)
+// and squared s times.  M = 2^(tl - n2) X with tl = -tau mean log2(e); returns n2, the power of two
+// taken out.  For symmetric V this is the matrix the reference forms from eigh (pimc.py:1197-1205).
+template <int A>
+__device__ __forceinline__ int expm_neg_tau(const float (&am)[A][A], float tau, float (&M)[A][A]) {
+    float mean = 0.f;
+#pragma unroll
+    for (int i = 0; i < A; ++i) mean += am[i][i];
+    mean *= 1.f / float(A);
+    float B[A][A];
+    float nrm = 0.f;
+#pragma unroll
+    for (int r = 0; r < A; ++r) {
+        float rs = 0.f;
+#pragma unroll
+        for (int c = 0; c < A; ++c) {
+            B[r][c] = -tau * (am[r][c] - (r == c ? mean : 0.f));
+            rs += fabsf(B[r][c]);
+        }
+        nrm = fmaxf(nrm, rs);
+    }
+    int s = 0;
+    while (nrm > 0.5f && s < 40) { nrm *= 0.5f; ++s; }
+    const float sc = ldexpf(1.f, -s);
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) B[r][c] *= sc;
+    auto mul = [](const float (&X)[A][A], const float (&Y)[A][A], float (&Z)[A][A]) {
+#pragma unroll
+        for (int r = 0; r < A; ++r)
+#pragma unroll
+            for (int c = 0; c < A; ++c) {
+                float acc = 0.f;
+#pragma unroll
+                for (int m = 0; m < A; ++m) acc = fmaf(X[r][m], Y[m][c], acc);
+                Z[r][c] = acc;
+            }
+    };
+    float B2[A][A], B3[A][A], T1[A][A], X[A][A];
+    mul(B, B, B2);
+    mul(B2, B, B3);
+    constexpr float c3 = 1.f / 6.f, c4 = 1.f / 24.f, c5 = 1.f / 120.f, c6 = 1.f / 720.f, c7 = 1.f / 5040.f,
+                    c8 = 1.f / 40320.f;
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) T1[r][c] = (r == c ? c6 : 0.f) + c7 * B[r][c] + c8 * B2[r][c];
+    mul(T1, B3, X);
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) T1[r][c] = X[r][c] + (r == c ? c3 : 0.f) + c4 * B[r][c] + c5 * B2[r][c];
+    mul(T1, B3, X);
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) X[r][c] += (r == c ? 1.f : 0.f) + B[r][c] + 0.5f * B2[r][c];
+    for (int i = 0; i < s; ++i) {
+        mul(X, X, T1);
+#pragma unroll
+        for (int r = 0; r < A; ++r)
+#pragma unroll
+            for (int c = 0; c < A; ++c) X[r][c] = T1[r][c];
+    }
+    const float tl = -tau * mean * 1.4426950408889634f;
+    const float n2 = floorf(tl);
+    const float f = exp2f(tl - n2);
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c < A; ++c) M[r][c] = f * X[r][c];
+    return static_cast<int>(n2);
+}
+
 // Compensated (Kahan) FP32 sum for the per-chunk log accumulators; plain sum in FP64.
 template <typename T> struct LogSum;
 template <> struct LogSum<float> {
@@ -502,9 +579,17 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                         }
                     }
                 }
-                // ---- M = exp(-tau V) by Jacobi, warm-started from the previous bead ----
+                // ---- M = exp(-tau V): scaling and squaring in FP32, Jacobi (warm-started from the
+                //      previous bead) in the FP64 validation build ----
                 T M[A][A];
-                {
+                if constexpr (sizeof(T) == 4) {
+                    T am[A][A];
+#pragma unroll
+                    for (int b = 0; b < A; ++b)
+#pragma unroll
+                        for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
+                    nexp += expm_neg_tau<A>(am, static_cast<float>(m.tau), M);
+                } else {
                     const bool cold = ((p - p_begin) & 7) == 0;   // fresh basis every 8 beads
                     if (cold) {
 #pragma unroll
