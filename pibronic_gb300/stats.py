@@ -13,11 +13,13 @@ import math
 import numpy as np
 
 from . import _native
+from . import constants
 from . import jackknife as jk
 from .constants import boltzman
 
 __all__ = ["calculate_alpha_terms", "add_harmonic_contribution", "estimate_basic_properties",
-           "calculate_basic_property_terms", "device_estimates", "ess"]
+           "calculate_basic_property_terms", "basic_statistical_analysis", "alpha_statistical_analysis",
+           "basic_jackknife_analysis", "device_estimates", "ess"]
 
 
 def calculate_basic_property_terms(*args):
@@ -66,6 +68,30 @@ def add_harmonic_contribution(input_dict, E_sampling, Cv_sampling):
     """stats.py:126-130."""
     input_dict["E"] += E_sampling
     input_dict["Cv"] += Cv_sampling
+
+
+def _result_arrays(pimc_result):
+    return [pimc_result.scaled_rho, pimc_result.scaled_g, pimc_result.scaled_gofr_plus,
+            pimc_result.scaled_gofr_minus]
+
+
+def basic_statistical_analysis(temperature, pimc_result, analytic_data, delta_beta=constants.delta_beta):
+    """stats.py:182-196: Z, E, Cv from a BoxResultPM and the sampling model's analytic data (as
+    written by analytic.analytic_of_sampling_model and read by analytic.load_analytic_data)."""
+    terms = calculate_basic_property_terms(delta_beta, *_result_arrays(pimc_result))
+    out = estimate_basic_properties(pimc_result.samples, temperature, *terms)
+    add_harmonic_contribution(out, analytic_data["E"], analytic_data["Cv"])
+    return out
+
+
+def alpha_statistical_analysis(temperature, pimc_result, analytic_data, delta_beta=constants.delta_beta):
+    """stats.py:199-216: the alpha estimator, g(beta +- dbeta) / rho weighted by the closed-form
+    alpha_pm = Z_rho(beta) / Z_rho(beta +- dbeta) of the sampling model."""
+    terms = calculate_alpha_terms(delta_beta, *_result_arrays(pimc_result), analytic_data["alpha_plus"],
+                                  analytic_data["alpha_minus"])
+    out = estimate_basic_properties(pimc_result.samples, temperature, *terms[:-4])
+    add_harmonic_contribution(out, analytic_data["E"], analytic_data["Cv"])
+    return out
 
 
 def basic_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta):
