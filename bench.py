@@ -502,23 +502,12 @@ def large_leg(args):
     learned proposal (flow over 2 ring slots per mode) is trained on the method's own samples."""
     import ctypes
     import torch
-    from pibronic_gb300 import _native, constants, pimc, stats, synthetic, vibronic_io
-    from pibronic_gb300.file_structure import FileStructure
+    from pibronic_gb300 import _native, stats
     from pibronic_gb300.flow import FlowProposal
     from pibronic_gb300.pimc import evaluate_device
     A, N, P, T = 12, 64, 256, 300.0
     X = args.large_samples
-    root = tempfile.mkdtemp(prefix="pbr_large_")
-    FS = FileStructure(root, 0, 0)
-    model = synthetic.make_coupled_model(A, N, 5, sd_quadratic=0.001)
-    vibronic_io.save_model_to_JSON(FS.path_vib_model, model)
-    vibronic_io.create_basic_diagonal_model(FS)
-    data = pimc.BoxDataPM(1e-4 * constants.beta(T))
-    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
-    data.states, data.modes, data.beads, data.temperature = A, N, P, T
-    data.samples = data.block_size = 1000
-    data.blocks = 1
-    data.preprocess()
+    data = large_model_data(T)
     plan = data.plan
     assert plan.use_tc
     evaluate_device(plan, 1000, seed=9, offset=0)
@@ -591,6 +580,38 @@ def large_leg(args):
     return out
 
 
+def large_model_data(T=300.0):
+    """The large dense configuration's model pair and BoxDataPM (A=12, N=64, P=256, dense Q)."""
+    from pibronic_gb300 import constants, pimc, synthetic, vibronic_io
+    from pibronic_gb300.file_structure import FileStructure
+    A, N, P = 12, 64, 256
+    FS = FileStructure(tempfile.mkdtemp(prefix="pbr_large_"), 0, 0)
+    model = synthetic.make_coupled_model(A, N, 5, sd_quadratic=0.001)
+    vibronic_io.save_model_to_JSON(FS.path_vib_model, model)
+    vibronic_io.create_basic_diagonal_model(FS)
+    data = pimc.BoxDataPM(1e-4 * constants.beta(T))
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.states, data.modes, data.beads, data.temperature = A, N, P, T
+    data.samples = data.block_size = 1000
+    data.blocks = 1
+    data.preprocess()
+    return data
+
+
+def profile_large(args):
+    """Profiling helper (no timing, no JSON line): two evaluations of args.profile_large samples of
+    the large dense configuration through the tensor-core form, for an ncu capture."""
+    import torch
+    from pibronic_gb300.pimc import evaluate_device
+    data = large_model_data()
+    for i in range(2):
+        out = evaluate_device(data.plan, args.profile_large, seed=1 + i, offset=0)
+    torch.cuda.synchronize()
+    assert int(out["status"].item()) == 0
+    print("profile-large done", args.profile_large)
+    return 0
+
+
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
     each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
@@ -637,7 +658,11 @@ def main():
     ap.add_argument("--batch-samples", type=int, default=100_000)
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--large-samples", type=int, default=400_000)
+    ap.add_argument("--profile-large", type=int, default=0,
+                    help="profiling helper: evaluate this many samples of the large configuration twice, exit")
     args = ap.parse_args()
+    if args.profile_large > 0:
+        return profile_large(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
