@@ -58,14 +58,12 @@ __host__ __device__ inline int rec_len(int A, int K) {
 
 // Shared-memory plan (in elements of the table type, esz bytes each); identical on host and device.
 struct SmemPlan {
-    int c, e, qq, poff, rc, rec, q, qlo, total_bytes;
+    int c, e, qq, rc, rec, q, qlo, total_bytes;
     __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int S, int qstride) {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P);
-        poff = take(2 * npair(N));          // per mode pair (d >= e): the q offsets d * rs, e * rs
-        rc = take(A);
+        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
         rec = take(N * rec_len(A, K));
         q = take(S * qstride);
         qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
@@ -187,6 +185,13 @@ __device__ __forceinline__ void jacobi_accumulate(T (&a)[A][A], T (&u)[A][A], in
         }
     }
 }
+
+// Forms chosen at compile time from measurements: the register exponential below replaces the
+// Jacobi eigensolver from 3 surfaces on (a 2 x 2 Jacobi is a single exact rotation), and the
+// quadratic part of V runs as one flat loop over the mode pairs from 4 surfaces on (below that the
+// pair-index bookkeeping outweighs the few FMAs per pair).
+constexpr int kExpmMinA = 3;
+constexpr int kFlatPairsMinA = 4;
 
 // exp(-tau V) for a small symmetric V held in registers (FP32): V is shifted by its mean
 // eigenvalue (trace / A), scaled by 2^-s until ||tau (V - mean)||_inf <= 1/2, exponentiated by the
@@ -409,14 +414,6 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
             s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
         }
         for (int i = threadIdx.x; i < A; i += blockDim.x) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
-        {
-            int* s_poff = reinterpret_cast<int*>(sm + plan.poff);
-            for (int d = threadIdx.x; d < N; d += blockDim.x)
-                for (int e = 0; e <= d; ++e) {
-                    s_poff[2 * pair_index(d, e)] = d * rs;
-                    s_poff[2 * pair_index(d, e) + 1] = e * rs;
-                }
-        }
         for (int i = threadIdx.x; i < N * MR; i += blockDim.x) {
             const int j = i / MR, o = i - j * MR;
             T v = T(0);
@@ -575,25 +572,39 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                     for (int k = 0; k <= K; ++k) osr[k][a] = e0 * ek[k];
                 }
-                // ---- quadratic part of V: one flat loop over the mode pairs (offsets from the
-                //      pair table), unrolled so several pairs' loads are in flight together ----
-                {
-                    const int* s_poff = reinterpret_cast<const int*>(sm + plan.poff);
+                // ---- quadratic part of V: one flat loop over the mode pairs (d, e <= d) in table
+                //      order, unrolled so several pairs' loads are in flight together ----
+                if constexpr (A >= kFlatPairsMinA) {
                     const int N2 = npair(N);
+                    int od = 0, oe = 0;                  // offsets d * rs, e * rs of the pair (d, e)
 #pragma unroll 4
                     for (int row = 0; row < N2; ++row) {
-                        const int2 o = *reinterpret_cast<const int2*>(s_poff + 2 * row);
-                        const T w = qs[ip + o.x] * qs[ip + o.y];
+                        const T w = qs[ip + od] * qs[ip + oe];
                         T qrow[A2P];
                         ldv(s_qq + row * A2P, qrow);
 #pragma unroll
                         for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                        const bool wrap = (oe == od);        // e == d: next row starts (d + 1, 0)
+                        od = wrap ? od + rs : od;
+                        oe = wrap ? 0 : oe + rs;
+                    }
+                } else {
+                    int row = 0;
+                    for (int d = 0; d < N; ++d) {
+                        const T qd = qs[ip + d * rs];
+                        for (int e = 0; e <= d; ++e, ++row) {
+                            const T w = qd * qs[ip + e * rs];
+                            T qrow[A2P];
+                            ldv(s_qq + row * A2P, qrow);
+#pragma unroll
+                            for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                        }
                     }
                 }
                 // ---- M = exp(-tau V): scaling and squaring in FP32, Jacobi (warm-started from the
                 //      previous bead) in the FP64 validation build ----
                 T M[A][A];
-                if constexpr (sizeof(T) == 4) {
+                if constexpr (sizeof(T) == 4 && A >= kExpmMinA) {
                     T am[A][A];
 #pragma unroll
                     for (int b = 0; b < A; ++b)

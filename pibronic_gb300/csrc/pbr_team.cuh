@@ -21,6 +21,9 @@
 namespace pbr {
 
 constexpr int kTeamThreads = 256;
+// largest surface count whose exp(-tau V) is formed by scaling and squaring in one thread's
+// registers (FP32); beyond it the per-thread Jacobi of the FP64 form is used
+constexpr int kTeamExpmMaxA = 6;
 
 struct TeamArgs {
     pbr_model m;
@@ -49,17 +52,15 @@ __host__ __device__ inline int pow2_ceil(int x) {
 __host__ __device__ inline int record_len(int A, int K) { return align_up(A * A + (K + 1) * A + 2 + A, 4); }
 
 struct TeamPlan {
-    int c, e, qq, poff, rc, rec, src, q, qlo, beads, lsums, total_bytes;
-    __host__ __device__ TeamPlan() : c(0), e(0), qq(0), poff(0), rc(0), rec(0), src(0), q(0), qlo(0), beads(0),
+    int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
+    __host__ __device__ TeamPlan() : c(0), e(0), qq(0), rc(0), rec(0), src(0), q(0), qlo(0), beads(0),
                                      lsums(0), total_bytes(0) {}
     __host__ __device__ TeamPlan(int A, int K, int qm, int esz, int N, int P, int S, int G, int qstride,
                                  int rl) {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        c = take((K + 1) * A); e = take(A2P); qq = take(qm == kQ32V ? 0 : npair(N) * A2P);
-        poff = take(qm == kQ32V ? 0 : 2 * npair(N) * (esz == 4 ? 1 : 1));   // mode-pair q offsets (ints)
-        rc = take(A);
+        c = take((K + 1) * A); e = take(A2P); qq = take(qm == kQ32V ? 0 : npair(N) * A2P); rc = take(A);
         rec = take(N * rec_len(A, K));
         src = take(S);                                             // ints stored in the slot
         q = take(S * qstride);
@@ -75,7 +76,7 @@ struct TeamPlan {
 
 // Copy one model's tables into the CTA's shared memory (layout TeamPlan).
 template <int A, int K, int QM, typename T>
-__device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan, int rs) {
+__device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
     constexpr int KP = (K + 1 + 3) / 4 * 4;
@@ -101,14 +102,6 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
             s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
         }
         for (int i = tid; i < A; i += NT) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
-        if (QM != kQ32V) {
-            int* s_poff = reinterpret_cast<int*>(sm + plan.poff);
-            for (int d = tid; d < N; d += NT)
-                for (int e = 0; e <= d; ++e) {
-                    s_poff[2 * pair_index(d, e)] = d * rs;
-                    s_poff[2 * pair_index(d, e) + 1] = e * rs;
-                }
-        }
         for (int i = tid; i < N * MR; i += NT) {
             const int j = i / MR, o = i - j * MR;
             T v = T(0);
@@ -300,20 +293,49 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     if (pr + 3 < A2) v[pr + 3] = T(w.w);
                 }
             } else {
-                // one flat loop over the mode pairs, unrolled so several pairs' loads are in flight
-                const int* s_poff = reinterpret_cast<const int*>(sm + plan.poff);
-                const int N2 = npair(N);
+                // one flat loop over the mode pairs (d, e <= d) in table order, unrolled so several
+                // pairs' loads are in flight together
+                if constexpr (A >= kFlatPairsMinA) {
+                    const int N2 = npair(N);
+                    int od = 0, oe = 0;                  // offsets d * rs, e * rs of the pair (d, e)
 #pragma unroll 4
-                for (int row = 0; row < N2; ++row) {
-                    const int2 o = *reinterpret_cast<const int2*>(s_poff + 2 * row);
-                    const T w = qs[ip + o.x] * qs[ip + o.y];
-                    T qrow[A2P];
-                    ldv(s_qq + row * A2P, qrow);
+                    for (int row = 0; row < N2; ++row) {
+                        const T w = qs[ip + od] * qs[ip + oe];
+                        T qrow[A2P];
+                        ldv(s_qq + row * A2P, qrow);
 #pragma unroll
-                    for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                        for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                        const bool wrap = (oe == od);        // e == d: next row starts (d + 1, 0)
+                        od = wrap ? od + rs : od;
+                        oe = wrap ? 0 : oe + rs;
+                    }
+                } else {
+                    int row = 0;
+                    for (int d = 0; d < N; ++d) {
+                        const T qd = qs[ip + d * rs];
+                        for (int e = 0; e <= d; ++e, ++row) {
+                            const T w = qd * qs[ip + e * rs];
+                            T qrow[A2P];
+                            ldv(s_qq + row * A2P, qrow);
+#pragma unroll
+                            for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                        }
+                    }
                 }
             }
-            {
+            if constexpr (sizeof(T) == 4 && A >= kExpmMinA && A <= kTeamExpmMaxA) {
+                // M = exp(-tau V) by scaling and squaring in registers (see expm_neg_tau)
+                T am[A][A], Mx[A][A];
+#pragma unroll
+                for (int b = 0; b < A; ++b)
+#pragma unroll
+                    for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
+                rec_out[OFF_N] = T(expm_neg_tau<A>(am, static_cast<float>(m.tau), Mx));
+#pragma unroll
+                for (int b = 0; b < A; ++b)
+#pragma unroll
+                    for (int c = 0; c < A; ++c) rec_out[b * A + c] = Mx[b][c];
+            } else {
                 T am[A][A], u[A][A];
 #pragma unroll
                 for (int b = 0; b < A; ++b)
@@ -561,7 +583,7 @@ __global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kern
     T* sm = reinterpret_cast<T*>(smem_raw);
     const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
                         args.qstride, args.rl);
-    team_load_tables<A, K, QM, T>(args.m, sm, plan, args.rs);
+    team_load_tables<A, K, QM, T>(args.m, sm, plan);
     __syncthreads();
     for (int64_t base = static_cast<int64_t>(blockIdx.x) * args.S; base < args.X;
          base += static_cast<int64_t>(gridDim.x) * args.S)
@@ -596,7 +618,7 @@ pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int
         const TeamArgs& a = items[lo].a;
         if (lo != cur) {
             plan = TeamPlan(A, K, kSample, 4, a.m.N, a.m.P, a.S, a.G, a.qstride, a.rl);
-            team_load_tables<A, K, kSample, float>(a.m, sm, plan, a.rs);
+            team_load_tables<A, K, kSample, float>(a.m, sm, plan);
             __syncthreads();
             cur = lo;
         }
