@@ -46,11 +46,14 @@ __device__ __forceinline__ float u01(uint32_t v) {
     return (static_cast<float>(v >> 8) + 0.5f) * (1.0f / 16777216.0f);
 }
 
-// two standard normals from two uniforms (Box-Muller)
+// two standard normals from two uniforms (Box-Muller), with the hardware-approximate log and
+// sine / cosine: u01 keeps the log's argument in (0, 1] and the angle in (0, 2 pi), where both are
+// accurate to about 1e-6 -- far below what a Gaussian draw needs, and the draws stay a function of
+// the counter alone (every kernel form calls this function)
 __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, float& z1) {
-    float r = sqrtf(-2.0f * logf(u01(a)));
+    const float r = sqrtf(-2.0f * __logf(u01(a)));
     float s, c;
-    sincospif(2.0f * u01(b), &s, &c);
+    __sincosf(6.283185307179586f * u01(b), &s, &c);
     z0 = r * c;
     z1 = r * s;
 }
