@@ -382,35 +382,54 @@ __global__ void flow_layer_bwd_kernel(const LayerDev L, int64_t X, float* __rest
     }
 }
 
-// C[M][N] (+)= sum_x A[x][M] B[x][N]: block = 32 x 32 tile x one batch split; partials reduced in
-// split order by gemm_tn_reduce.
-constexpr int kTile = 32;
-__global__ void gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B, int64_t X, int M,
-                                int N, int64_t chunk, float* __restrict__ part) {
-    __shared__ float sa[kTile][kTile + 1], sb[kTile][kTile + 1];
-    const int tm = blockIdx.x * kTile, tn = blockIdx.y * kTile, split = blockIdx.z;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+// C[M][N] (+)= sum_x A[x][M] B[x][N] (the weight gradients: the batch is the reduction): a block
+// computes a 64 x 64 tile of C over one contiguous split of the batch, 256 threads with 4 x 4
+// outputs each from register-blocked outer products (two 128-bit shared loads per 16 FMAs); the
+// splits' partials are added in split order by gemm_tn_reduce, so the result is deterministic.
+constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
+constexpr int kGemmRowsPerSplit = 256;
+__global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B,
+                                                       int64_t X, int M, int N, int64_t chunk,
+                                                       float* __restrict__ part) {
+    __shared__ __align__(16) float sa[kGBK][kGBM + kGPad];
+    __shared__ __align__(16) float sb[kGBK][kGBN + kGPad];
+    const int tm = blockIdx.x * kGBM, tn = blockIdx.y * kGBN, split = blockIdx.z;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;       // 16 x 16 threads, 4 x 4 outputs each
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
     const int64_t x0 = split * chunk, x1 = min(X, x0 + chunk);
-    for (int64_t xb = x0; xb < x1; xb += kTile) {
-        for (int r = ty; r < kTile; r += 8) {
+    for (int64_t xb = x0; xb < x1; xb += kGBK) {
+        for (int i = threadIdx.x; i < kGBK * kGBM; i += 256) {
+            const int r = i / kGBM, c = i - r * kGBM;
             const int64_t xx = xb + r;
-            sa[r][tx] = (xx < x1 && tm + tx < M) ? A[xx * M + tm + tx] : 0.f;
-            sb[r][tx] = (xx < x1 && tn + tx < N) ? B[xx * N + tn + tx] : 0.f;
+            sa[r][c] = (xx < x1 && tm + c < M) ? A[xx * M + tm + c] : 0.f;
+            sb[r][c] = (xx < x1 && tn + c < N) ? B[xx * N + tn + c] : 0.f;
         }
         __syncthreads();
 #pragma unroll 8
-        for (int r = 0; r < kTile; ++r) {
-            const float bv = sb[r][tx];
+        for (int k = 0; k < kGBK; ++k) {
+            const float4 a = *reinterpret_cast<const float4*>(&sa[k][ty * 4]);
+            const float4 b = *reinterpret_cast<const float4*>(&sb[k][tx * 4]);
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-            for (int u = 0; u < 4; ++u) acc[u] = fmaf(sa[r][ty + 8 * u], bv, acc[u]);
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int m = tm + ty + 8 * u, n = tn + tx;
-        if (m < M && n < N) part[(static_cast<int64_t>(split) * M + m) * N + n] = acc[u];
+    for (int i = 0; i < 4; ++i) {
+        const int m = tm + ty * 4 + i;
+        if (m >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int n = tn + tx * 4 + j;
+            if (n < N) part[(static_cast<int64_t>(split) * M + m) * N + n] = acc[i][j];
+        }
     }
 }
 
@@ -623,7 +642,8 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
 }
 
 int64_t pbr_gemm_tn_scratch(int64_t X, int32_t M, int32_t N) {
-    const int64_t splits = X < 64 * kTile ? 1 : (X / (64 * kTile) < 64 ? X / (64 * kTile) : 64);
+    const int64_t s = X / kGemmRowsPerSplit;
+    const int64_t splits = s < 1 ? 1 : (s < 64 ? s : 64);
     return splits * static_cast<int64_t>(M) * N;
 }
 
@@ -633,7 +653,7 @@ int pbr_gemm_tn_acc(const float* A, const float* B, int64_t X, int32_t M, int32_
     const int64_t splits = pbr_gemm_tn_scratch(X, M, N) / (static_cast<int64_t>(M) * N);
     const int64_t chunk = (X + splits - 1) / splits;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    dim3 grid((M + kTile - 1) / kTile, (N + kTile - 1) / kTile, static_cast<unsigned>(splits));
+    dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, static_cast<unsigned>(splits));
     gemm_tn_partial<<<grid, 256, 0, st>>>(A, B, X, M, N, chunk, scratch);
     gemm_tn_reduce<<<grid_for(static_cast<int64_t>(M) * N, 256), 256, 0, st>>>(scratch, static_cast<int>(splits),
                                                                                M * N, beta, C);
