@@ -382,6 +382,319 @@ __global__ void flow_layer_bwd_kernel(const LayerDev L, int64_t X, float* __rest
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Sample-tiled coupling layers (the form used whenever the padded weights fit in shared memory).
+// A block takes 64 samples at a time and runs the conditioner's three dense layers as
+// register-blocked shared-memory GEMMs: 16 x 16 threads, each owning 4 samples x 4*CB columns of
+// a 64*CB-wide column block, so one 128-bit load of activations and CB 128-bit loads of weights
+// feed 16*CB FMAs.  Weights stay resident, zero-padded: hidden width Hp = roundup(H, 64*HB)
+// (HB = 1 or 2, H <= 128), head width Op = roundup(2J, 64) with the columns of s_j and t_j
+// interleaved (2j, 2j+1) so a thread holds both halves of its coupling pairs.  Activation tiles
+// are row-major with a row stride of 4 mod 8 floats: the two sample rows a warp reads at once fall
+// in different banks.
+// ---------------------------------------------------------------------------------------------
+constexpr int kTileS = 64;
+constexpr int kTileThreads = 256;
+
+struct TileDims {
+    int I4, Hp, Op, Ip, ldya, ldh, ldo;
+    __host__ __device__ TileDims(int I, int J, int H, int HB)
+        : I4(align_up_(I, 4)), Hp(align_up_(H, 64 * HB)), Op(align_up_(2 * J, 64)), Ip(align_up_(I, 64)),
+          ldya(align_up_(align_up_(I, 4), 8) + 4), ldh(align_up_(H, 64 * HB) + 4), ldo(align_up_(2 * J, 64) + 4) {}
+    __host__ __device__ int fwd_floats() const {
+        return I4 * Hp + Hp * Hp + Hp * Op + 2 * Hp + Op + kTileS * (ldya + ldh);
+    }
+    __host__ __device__ int bwd_floats() const { return Op * Hp + Hp * Hp + Hp * Ip + kTileS * (ldo + ldh); }
+};
+
+__device__ __forceinline__ float f4c(const float4& v, int i) {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// acc[r][4u + v] += sum_{k < K4} in[(4 sg + r) ld_in + k] * w[k ld_w + c0 + 4 cg + 64 u + v]
+template <int CB>
+__device__ __forceinline__ void tile_gemm(const float* __restrict__ in, int ld_in, int K4,
+                                          const float* __restrict__ w, int ld_w, int c0, int sg, int cg,
+                                          float (&acc)[4][4 * CB]) {
+    const float* a_row = in + 4 * sg * ld_in;
+    const float* w_col = w + c0 + 4 * cg;
+#pragma unroll 2
+    for (int k = 0; k < K4; k += 4) {
+        float4 a[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = *reinterpret_cast<const float4*>(a_row + r * ld_in + k);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+#pragma unroll
+            for (int u = 0; u < CB; ++u) {
+                const float4 wv = *reinterpret_cast<const float4*>(w_col + (k + kk) * ld_w + 64 * u);
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const float av = f4c(a[r], kk);
+                    acc[r][4 * u + 0] = fmaf(av, wv.x, acc[r][4 * u + 0]);
+                    acc[r][4 * u + 1] = fmaf(av, wv.y, acc[r][4 * u + 1]);
+                    acc[r][4 * u + 2] = fmaf(av, wv.z, acc[r][4 * u + 2]);
+                    acc[r][4 * u + 3] = fmaf(av, wv.w, acc[r][4 * u + 3]);
+                }
+            }
+        }
+    }
+}
+
+template <int CB>
+__device__ __forceinline__ void tile_init(float (&acc)[4][4 * CB], const float* __restrict__ bias, int c0, int cg) {
+#pragma unroll
+    for (int u = 0; u < CB; ++u) {
+        const float4 b = bias ? *reinterpret_cast<const float4*>(bias + c0 + 4 * cg + 64 * u)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            acc[r][4 * u + 0] = b.x; acc[r][4 * u + 1] = b.y; acc[r][4 * u + 2] = b.z; acc[r][4 * u + 3] = b.w;
+        }
+    }
+}
+
+template <int HB>
+__global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_kernel(const LayerDev L, int dir, int64_t X,
+                                                                     float* __restrict__ y,
+                                                                     double* __restrict__ logdet,
+                                                                     const SaveDev sv) {
+    extern __shared__ __align__(16) float fsm[];
+    const int I = L.I, J = L.J, H = L.H, D = L.D;
+    const TileDims td(I, J, H, HB);
+    const int Hp = td.Hp, Op = td.Op, I4 = td.I4, ldya = td.ldya, ldh = td.ldh;
+    float* w1 = fsm;                      // [I4][Hp]
+    float* w2 = w1 + I4 * Hp;             // [Hp][Hp]
+    float* w3 = w2 + Hp * Hp;             // [Hp][Op], (s_j, t_j) at columns (2j, 2j+1)
+    float* bb1 = w3 + Hp * Op;
+    float* bb2 = bb1 + Hp;
+    float* bb3 = bb2 + Hp;                // [Op], interleaved like w3
+    float* ya = bb3 + Op;                 // [64][ldya]
+    float* hs = ya + kTileS * ldya;       // [64][ldh]: h1, then h2
+    for (int i = threadIdx.x; i < I4 * Hp; i += blockDim.x) {
+        const int k = i / Hp, c = i - k * Hp;
+        w1[i] = (k < I && c < H) ? L.W1[k * H + c] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Hp * Hp; i += blockDim.x) {
+        const int k = i / Hp, c = i - k * Hp;
+        w2[i] = (k < H && c < H) ? L.W2[k * H + c] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Hp * Op; i += blockDim.x) {
+        const int k = i / Op, c = i - k * Op, j = c >> 1;
+        w3[i] = (k < H && j < J) ? L.W3[k * 2 * J + ((c & 1) ? J + j : j)] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Hp; i += blockDim.x) {
+        bb1[i] = i < H ? L.b1[i] : 0.f;
+        bb2[i] = i < H ? L.b2[i] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Op; i += blockDim.x) {
+        const int j = i >> 1;
+        bb3[i] = j < J ? L.b3[(i & 1) ? J + j : j] : 0.f;
+    }
+    const int sg = threadIdx.x >> 4, cg = threadIdx.x & 15;
+    const int64_t ntiles = (X + kTileS - 1) / kTileS;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t x0 = t * kTileS;
+        __syncthreads();                  // weights loaded / the previous tile's readers are done
+        for (int i = threadIdx.x; i < kTileS * I4; i += blockDim.x) {
+            const int s = i / I4, c = i - s * I4;
+            const int64_t x = x0 + s;
+            ya[s * ldya + c] = (c < I && x < X) ? y[x * D + __ldg(L.idx_a + c)] : 0.f;
+        }
+        __syncthreads();
+        if (sv.ya) {
+            for (int i = threadIdx.x; i < kTileS * I; i += blockDim.x) {
+                const int s = i / I, c = i - s * I;
+                if (x0 + s < X) sv.ya[(x0 + s) * I + c] = ya[s * ldya + c];
+            }
+        }
+        float acc[4][4 * HB];
+        // ---- h1 = tanh(ya W1 + b1) ----
+        tile_init<HB>(acc, bb1, 0, cg);
+        tile_gemm<HB>(ya, ldya, I4, w1, Hp, 0, sg, cg, acc);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t x = x0 + 4 * sg + r;
+#pragma unroll
+            for (int u = 0; u < HB; ++u) {
+                const int c = 4 * cg + 64 * u;
+                const float4 h = make_float4(tanhf(acc[r][4 * u]), tanhf(acc[r][4 * u + 1]),
+                                             tanhf(acc[r][4 * u + 2]), tanhf(acc[r][4 * u + 3]));
+                *reinterpret_cast<float4*>(hs + (4 * sg + r) * ldh + c) = h;
+                if (sv.h1 && x < X && c < H) *reinterpret_cast<float4*>(sv.h1 + x * H + c) = h;
+            }
+        }
+        __syncthreads();
+        // ---- h2 = tanh(h1 W2 + b2) ----
+        tile_init<HB>(acc, bb2, 0, cg);
+        tile_gemm<HB>(hs, ldh, Hp, w2, Hp, 0, sg, cg, acc);
+        __syncthreads();                  // every read of h1 is done
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t x = x0 + 4 * sg + r;
+#pragma unroll
+            for (int u = 0; u < HB; ++u) {
+                const int c = 4 * cg + 64 * u;
+                const float4 h = make_float4(tanhf(acc[r][4 * u]), tanhf(acc[r][4 * u + 1]),
+                                             tanhf(acc[r][4 * u + 2]), tanhf(acc[r][4 * u + 3]));
+                *reinterpret_cast<float4*>(hs + (4 * sg + r) * ldh + c) = h;
+                if (sv.h2 && x < X && c < H) *reinterpret_cast<float4*>(sv.h2 + x * H + c) = h;
+            }
+        }
+        __syncthreads();
+        // ---- head (s, t) = h2 W3 + b3 and the affine coupling of the b half ----
+        float lsum[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int cb = 0; cb < Op; cb += 64) {
+            float o[4][4];
+            tile_init<1>(o, bb3, cb, cg);
+            tile_gemm<1>(hs, ldh, Hp, w3, Op, cb, sg, cg, o);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int64_t x = x0 + 4 * sg + r;
+                if (x >= X) continue;
+#pragma unroll
+                for (int pp = 0; pp < 2; ++pp) {
+                    const int j = (cb >> 1) + 2 * cg + pp;
+                    if (j >= J) continue;
+                    const float sv_s = kKappa * tanhf(o[r][2 * pp] / kKappa);
+                    const float to = o[r][2 * pp + 1];
+                    const int bi = __ldg(L.idx_b + j);
+                    const float yb = y[x * D + bi];
+                    const float out = (dir > 0) ? fmaf(yb, __expf(sv_s), to) : (yb - to) * __expf(-sv_s);
+                    y[x * D + bi] = out;
+                    lsum[r] += sv_s;
+                    if (sv.s) { sv.s[x * J + j] = sv_s; sv.yb[x * J + j] = out; }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int o = 8; o >= 1; o >>= 1) lsum[r] += __shfl_xor_sync(0xffffffffu, lsum[r], o);
+        if (cg == 0) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int64_t x = x0 + 4 * sg + r;
+                if (x < X) logdet[x] += (dir > 0) ? static_cast<double>(lsum[r]) : -static_cast<double>(lsum[r]);
+            }
+        }
+    }
+}
+
+// Back-propagation through one layer of the inverse direction, tiled like the forward pass: the
+// coupling terms elementwise, then gz2 = (g_o W3^T) (1 - h2^2), gz1 = (gz2 W2^T) (1 - h1^2) and
+// dL/dya = gz1 W1^T as shared-memory GEMMs against the transposed weights.
+template <int HB>
+__global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const LayerDev L, int64_t X,
+                                                                     float* __restrict__ gy,
+                                                                     const float* __restrict__ rt,
+                                                                     const SaveDev sv, float* __restrict__ g_o,
+                                                                     float* __restrict__ g_z2,
+                                                                     float* __restrict__ g_z1) {
+    extern __shared__ __align__(16) float fsm[];
+    const int I = L.I, J = L.J, H = L.H, D = L.D, O = 2 * J;
+    const TileDims td(I, J, H, HB);
+    const int Hp = td.Hp, Op = td.Op, Ip = td.Ip, ldo = td.ldo, ldh = td.ldh;
+    float* w3t = fsm;                     // [Op][Hp]: row 2j + (0: s_j, 1: t_j) of W3^T
+    float* w2t = w3t + Op * Hp;           // [Hp][Hp] = W2^T
+    float* w1t = w2t + Hp * Hp;           // [Hp][Ip] = W1^T
+    float* go = w1t + Hp * Ip;            // [64][ldo]
+    float* gz = go + kTileS * ldo;        // [64][ldh]: gz2, then gz1
+    for (int i = threadIdx.x; i < Op * Hp; i += blockDim.x) {
+        const int c = i / Hp, h = i - c * Hp, j = c >> 1;
+        w3t[i] = (j < J && h < H) ? L.W3[h * O + ((c & 1) ? J + j : j)] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Hp * Hp; i += blockDim.x) {
+        const int m = i / Hp, h = i - m * Hp;
+        w2t[i] = (m < H && h < H) ? L.W2[h * H + m] : 0.f;
+    }
+    for (int i = threadIdx.x; i < Hp * Ip; i += blockDim.x) {
+        const int h = i / Ip, a = i - h * Ip;
+        w1t[i] = (h < H && a < I) ? L.W1[a * H + h] : 0.f;
+    }
+    const int sg = threadIdx.x >> 4, cg = threadIdx.x & 15;
+    const int OH = Op >> 1;
+    const int64_t ntiles = (X + kTileS - 1) / kTileS;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t x0 = t * kTileS;
+        __syncthreads();
+        // ---- coupling: dL/d(s, t) per pair, dL/dyb' in place ----
+        for (int i = threadIdx.x; i < kTileS * OH; i += blockDim.x) {
+            const int s = i / OH, j = i - s * OH;
+            const int64_t x = x0 + s;
+            float gos = 0.f, gt = 0.f;
+            if (j < J && x < X) {
+                const int bi = __ldg(L.idx_b + j);
+                const float sj = sv.s[x * J + j], yb = sv.yb[x * J + j];
+                const float gyb = gy[x * D + bi];
+                const float es = __expf(-sj);
+                gos = (-gyb * yb + rt[x]) * (1.0f - (sj / kKappa) * (sj / kKappa));
+                gt = -gyb * es;
+                gy[x * D + bi] = gyb * es;
+                g_o[x * O + j] = gos;
+                g_o[x * O + J + j] = gt;
+            }
+            go[s * ldo + 2 * j] = gos;
+            go[s * ldo + 2 * j + 1] = gt;
+        }
+        __syncthreads();
+        float acc[4][4 * HB];
+        // ---- gz2 ----
+        tile_init<HB>(acc, nullptr, 0, cg);
+        tile_gemm<HB>(go, ldo, Op, w3t, Hp, 0, sg, cg, acc);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t x = x0 + 4 * sg + r;
+#pragma unroll
+            for (int u = 0; u < HB; ++u) {
+                const int c = 4 * cg + 64 * u;
+                const bool ok = x < X && c < H;
+                const float4 h = ok ? *reinterpret_cast<const float4*>(sv.h2 + x * H + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 v = make_float4(acc[r][4 * u] * (1.f - h.x * h.x), acc[r][4 * u + 1] * (1.f - h.y * h.y),
+                                             acc[r][4 * u + 2] * (1.f - h.z * h.z), acc[r][4 * u + 3] * (1.f - h.w * h.w));
+                *reinterpret_cast<float4*>(gz + (4 * sg + r) * ldh + c) = v;
+                if (ok) *reinterpret_cast<float4*>(g_z2 + x * H + c) = v;
+            }
+        }
+        __syncthreads();
+        // ---- gz1 ----
+        tile_init<HB>(acc, nullptr, 0, cg);
+        tile_gemm<HB>(gz, ldh, Hp, w2t, Hp, 0, sg, cg, acc);
+        __syncthreads();                  // every read of gz2 is done
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int64_t x = x0 + 4 * sg + r;
+#pragma unroll
+            for (int u = 0; u < HB; ++u) {
+                const int c = 4 * cg + 64 * u;
+                const bool ok = x < X && c < H;
+                const float4 h = ok ? *reinterpret_cast<const float4*>(sv.h1 + x * H + c) : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 v = make_float4(acc[r][4 * u] * (1.f - h.x * h.x), acc[r][4 * u + 1] * (1.f - h.y * h.y),
+                                             acc[r][4 * u + 2] * (1.f - h.z * h.z), acc[r][4 * u + 3] * (1.f - h.w * h.w));
+                *reinterpret_cast<float4*>(gz + (4 * sg + r) * ldh + c) = v;
+                if (ok) *reinterpret_cast<float4*>(g_z1 + x * H + c) = v;
+            }
+        }
+        __syncthreads();
+        // ---- dL/dya = gz1 W1^T, added at the a half ----
+        for (int cb = 0; cb < Ip; cb += 64) {
+            float o[4][4];
+            tile_init<1>(o, nullptr, cb, cg);
+            tile_gemm<1>(gz, ldh, Hp, w1t, Ip, cb, sg, cg, o);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int64_t x = x0 + 4 * sg + r;
+                if (x >= X) continue;
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    const int a = cb + 4 * cg + v;
+                    if (a < I) gy[x * D + __ldg(L.idx_a + a)] += o[r][v];
+                }
+            }
+        }
+    }
+}
+
 // C[M][N] (+)= sum_x A[x][M] B[x][N] (the weight gradients: the batch is the reduction): a block
 // computes a 64 x 64 tile of C over one contiguous split of the batch, 256 threads with 4 x 4
 // outputs each from register-blocked outer products (two 128-bit shared loads per 16 FMAs); the
@@ -545,6 +858,27 @@ bool layer_ok(const pbr_flow_layer* l) {
            l->idx_b && l->W1 && l->b1 && l->W2 && l->b2 && l->W3 && l->b3;
 }
 
+// Shared memory of the sample-tiled layer kernels, or 0 when they do not apply (H > 128, or the
+// padded weights and tiles exceed a block's shared memory): the warp-per-sample kernels then run.
+int tile_smem(const pbr_flow_layer* l, bool fwd) {
+    if (l->H > 128) return 0;
+    const TileDims td(l->I, l->J, l->H, l->H > 64 ? 2 : 1);
+    const int64_t bytes = static_cast<int64_t>(sizeof(float)) * (fwd ? td.fwd_floats() : td.bwd_floats());
+    return bytes <= 227 * 1024 ? static_cast<int>(bytes) : 0;
+}
+
+// persistent grid: one block per resident slot, no more blocks than tiles; 0 when it cannot run
+template <typename K>
+int tile_grid(K kern, int bytes, int64_t X) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return 0;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTileThreads, bytes) != cudaSuccess || occ < 1)
+        return 0;
+    const int64_t tiles = (X + kTileS - 1) / kTileS;
+    const int64_t cap = static_cast<int64_t>(sm_count()) * occ;
+    return static_cast<int>(tiles < cap ? tiles : cap);
+}
+
 LayerDev to_dev(const pbr_flow_layer* l) {
     return LayerDev{l->D, l->I, l->J, l->H, l->idx_a, l->idx_b, l->W1, l->b1, l->W2, l->b2, l->W3, l->b3};
 }
@@ -589,6 +923,17 @@ int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64
         if (!save->ya || !save->h1 || !save->h2 || !save->s || !save->yb) return PBR_ERR_ARG;
         sv = SaveDev{save->ya, save->h1, save->h2, save->s, save->yb};
     }
+    const int tb = tile_smem(layer, true);
+    if (tb > 0) {
+        auto run = [&](auto kern) -> int {
+            const int grid = tile_grid(kern, tb, X);
+            if (grid < 1) return PBR_ERR_UNSUPPORTED;
+            kern<<<grid, kTileThreads, tb, static_cast<cudaStream_t>(stream)>>>(to_dev(layer), direction, X, y,
+                                                                                 logdet, sv);
+            return status();
+        };
+        return layer->H > 64 ? run(flow_tile_fwd_kernel<2>) : run(flow_tile_fwd_kernel<1>);
+    }
     const int bytes = layer_smem_fwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
     auto go = [&](auto kern) -> int {
@@ -617,9 +962,20 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
     if (!layer_ok(layer) || !gy || !rt || !save || !g_o || !g_z2 || !g_z1 || X < 0) return PBR_ERR_ARG;
     if (!save->h1 || !save->h2 || !save->s || !save->yb) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
+    const SaveDev sv{save->ya, save->h1, save->h2, save->s, save->yb};
+    const int tb = tile_smem(layer, false);
+    if (tb > 0) {
+        auto run = [&](auto kern) -> int {
+            const int grid = tile_grid(kern, tb, X);
+            if (grid < 1) return PBR_ERR_UNSUPPORTED;
+            kern<<<grid, kTileThreads, tb, static_cast<cudaStream_t>(stream)>>>(to_dev(layer), X, gy, rt, sv, g_o,
+                                                                                 g_z2, g_z1);
+            return status();
+        };
+        return layer->H > 64 ? run(flow_tile_bwd_kernel<2>) : run(flow_tile_bwd_kernel<1>);
+    }
     const int bytes = layer_smem_bwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
-    const SaveDev sv{save->ya, save->h1, save->h2, save->s, save->yb};
     auto go = [&](auto kern) -> int {
         if (bytes > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)

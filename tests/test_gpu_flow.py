@@ -57,11 +57,19 @@ def test_prepare_matches_numpy(tmp_path):
     assert np.allclose(U.cpu().numpy(), Uref, rtol=1e-6, atol=1e-6)
 
 
-def test_layers_match_oracle(tmp_path):
+# (N, nsel, layers, hidden, X): sample-tiled layers at hidden 32 / 64 / 128 (ragged last tile, odd
+# D with I != J, the learned configurations' D = 60 and D = 128), and D = 192 at hidden 128, whose
+# padded weights exceed the tiled form's shared memory (the warp-per-sample layers run)
+LAYER_CASES = [(4, 3, 4, 64, 300), (5, 3, 2, 128, 77), (20, 3, 2, 128, 1000), (64, 2, 2, 128, 130),
+               (64, 3, 2, 128, 130), (4, 3, 2, 32, 65)]
+
+
+@pytest.mark.parametrize("N,nsel,layers,hidden,X", LAYER_CASES)
+def test_layers_match_oracle(tmp_path, N, nsel, layers, hidden, X):
     from oracle import flow_oracle as fo
-    FS, data = _box(tmp_path, A=2, N=4, P=12, X=64)
-    fl = _flow(data, nsel=3, layers=4, hidden=64, init_scale=0.5, seed=2)
-    y = torch.randn((300, fl.D), device="cuda")
+    FS, data = _box(tmp_path, A=2, N=N, P=12, X=64)
+    fl = _flow(data, nsel=nsel, layers=layers, hidden=hidden, init_scale=0.5, seed=2)
+    y = torch.randn((X, fl.D), device="cuda")
     yf, ldf = fl.forward(y)
     ref_y, ref_ld = fo.forward(fl.params_host(), y.double().cpu().numpy())
     assert np.allclose(yf.cpu().numpy(), ref_y, rtol=1e-4, atol=1e-4)
@@ -71,20 +79,22 @@ def test_layers_match_oracle(tmp_path):
     assert np.allclose(ldi.cpu().numpy(), -ldf.cpu().numpy(), atol=1e-4)
 
 
-def test_gradients_match_oracle(tmp_path):
+@pytest.mark.parametrize("N,nsel,layers,hidden,X", [(4, 3, 4, 32, 4096), (5, 3, 2, 128, 1000),
+                                                    (64, 2, 2, 128, 1000), (64, 3, 2, 128, 300)])
+def test_gradients_match_oracle(tmp_path, N, nsel, layers, hidden, X):
     from oracle import flow_oracle as fo
-    FS, data = _box(tmp_path, A=3, N=4, P=12, X=64)
-    fl = _flow(data, nsel=3, layers=4, hidden=32, init_scale=0.5, seed=5)
+    FS, data = _box(tmp_path, A=3, N=N, P=12, X=64)
+    fl = _flow(data, nsel=nsel, layers=layers, hidden=hidden, init_scale=0.5, seed=5)
     fl.nu.copy_(torch.tensor([0.2, -0.1, 0.3], device="cuda"))
-    y = torch.randn((4096, fl.D), device="cuda")
-    r = torch.exp(torch.randn(4096, device="cuda", dtype=torch.float64))
+    y = torch.randn((X, fl.D), device="cuda")
+    r = torch.exp(torch.randn(X, device="cuda", dtype=torch.float64))
     loss, grads, g_nu = fl.gradients(y, r)
     torch.cuda.synchronize()
     ref_loss, ref_grads, ref_gnu = fo.loss_and_grads(fl.params_host(), fl.nu.double().cpu().numpy(),
                                                      y.double().cpu().numpy(), r.cpu().numpy(),
                                                      fl.t_mu.double().cpu().numpy(), fl.log_w)
     assert math.isclose(float(loss), ref_loss, rel_tol=1e-4, abs_tol=1e-5)
-    for l in range(4):
+    for l in range(layers):
         for k, v in grads[l].items():
             ref = ref_grads[l][k]
             scale = np.abs(ref).max() + 1e-12
