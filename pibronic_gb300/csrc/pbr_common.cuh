@@ -61,6 +61,31 @@ __device__ __forceinline__ void box_muller(uint32_t a, uint32_t b, float& z0, fl
 // ----------------------------------------------------------------------------------------------
 // small helpers
 // ----------------------------------------------------------------------------------------------
+
+// d * 2^n, exact (as ldexp) -- one FP64 multiply by a power of two built from its exponent bits
+// when n is a normal exponent, ldexp otherwise
+__device__ __forceinline__ double scale_pow2(double d, int n) {
+    if (n >= -1022 && n <= 1023) return d * __longlong_as_double(static_cast<long long>(n + 1023) << 52);
+    return ldexp(d, n);
+}
+
+// e^x for the per-sample FP64 outputs of the FP32 kernels, whose arguments are sums of FP32 terms
+// (absolute error ~1e-6 and above): e^x = 2^n 2^f, n = floor(x log2 e) applied exactly and
+// 2^f (0 <= f < 1) from exp2f (relative error ~2e-7); extreme or non-finite x takes exp.  A few
+// FP64 operations instead of a full FP64 exponential, on a part whose FP64 rate is a small
+// fraction of its FP32 rate.
+__device__ __forceinline__ double exp_out_fp32(double x) {
+    const double t = x * 1.4426950408889634;
+    if (!(fabs(t) < 1000.0)) return exp(x);
+    const double n = floor(t);
+    return scale_pow2(static_cast<double>(exp2f(static_cast<float>(t - n))), static_cast<int>(n));
+}
+// the output exponential of a kernel computing in T: FP64 exp for the FP64 builds
+template <typename T>
+__device__ __forceinline__ double exp_out(double x) {
+    if constexpr (sizeof(T) == 8) return exp(x);
+    else return exp_out_fp32(x);
+}
 __host__ __device__ constexpr int npair(int n) { return n * (n + 1) / 2; }
 __host__ __device__ constexpr int pair_index(int b, int c) { return b * (b + 1) / 2 + c; }  // b >= c
 

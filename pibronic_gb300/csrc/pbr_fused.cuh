@@ -756,12 +756,12 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                 double tr = 0.0;
 #pragma unroll
                 for (int r = 0; r < A; ++r) tr += static_cast<double>(nser[k][r][r]);
-                coef[k] = ldexp(tr, nexp);
+                coef[k] = scale_pow2(tr, nexp);
             }
             double rho = 0.0;
 #pragma unroll
             for (int a = 0; a < A; ++a)
-                if (a < nfill) rho += exp(lr_d[a]);
+                if (a < nfill) rho += exp_out<T>(lr_d[a]);
             const pbr_outputs& o = args.out;
             o.s_rho[sidx] = rho;
             o.s_g[sidx] = coef[0];

@@ -545,9 +545,9 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                 if (r >= A) d = 0.0;
 #pragma unroll
                 for (int o = TA / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, TA);
-                coef[k] = ldexp(d, nexp);
+                coef[k] = scale_pow2(d, nexp);
             }
-            double rho = (r < A && r < nfill) ? exp(lr_d) : 0.0;
+            double rho = (r < A && r < nfill) ? exp_out<T>(lr_d) : 0.0;
 #pragma unroll
             for (int o = TA / 2; o >= 1; o >>= 1) rho += __shfl_xor_sync(tmask, rho, o, TA);
             if (r == 0) {

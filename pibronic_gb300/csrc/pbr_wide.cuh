@@ -474,9 +474,9 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
             double d = d0;
 #pragma unroll
             for (int o = kWideTeam / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, kWideTeam);
-            coef[k] = ldexp(d, nexp);
+            coef[k] = scale_pow2(d, nexp);
         }
-        double rho = (r < nfill) ? exp(lr_d) : 0.0;
+        double rho = (r < nfill) ? exp_out<float>(lr_d) : 0.0;
 #pragma unroll
         for (int o = kWideTeam / 2; o >= 1; o >>= 1) rho += __shfl_xor_sync(tmask, rho, o, kWideTeam);
         if (r == 0) {
