@@ -307,6 +307,22 @@ __device__ __forceinline__ int draw_source(const pbr_model& m, uint64_t sg, uint
 // handed to sink(p, q_p) for p = P-1 down to 0.  The FMAs are explicit so every kernel form
 // that draws through this function produces the same bits.  The distribution is rho's
 // N(d_src, Lambda^-1), the one the reference draws in normal modes.
+// one step of the back substitution: x_{P-1} = a z, else x_p = a_p (z_p - b_p x_{p+1} - c_p x_{P-1});
+// xnext <- x_p (and xlast <- x_p at p = P-1)
+template <typename T>
+__device__ __forceinline__ void chain_step(const T* __restrict__ a, const T* __restrict__ b,
+                                           const T* __restrict__ c, int p, int P, T z, T& xnext, T& xlast) {
+    T x;
+    if (p == P - 1) {
+        x = __ldg(a + p) * z;
+        xlast = x;
+    } else {
+        const T u = fma(-__ldg(b + p), xnext, z);
+        x = __ldg(a + p) * fma(-__ldg(c + p), xlast, u);
+    }
+    xnext = x;
+}
+
 template <typename T, typename Sink>
 __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, uint64_t sg, uint32_t key0,
                                                    uint32_t key1, T dsh, Sink&& sink) {
@@ -326,16 +342,8 @@ __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, ui
         for (int t = 3; t >= 0; --t) {
             const int p = 4 * p4 + t;
             if (p >= P) continue;
-            T x;
-            if (p == P - 1) {
-                x = __ldg(a + p) * T(z[t]);
-                xlast = x;
-            } else {
-                const T u = fma(-__ldg(b + p), xnext, T(z[t]));
-                x = __ldg(a + p) * fma(-__ldg(c + p), xlast, u);
-            }
-            xnext = x;
-            sink(p, x + dsh);
+            chain_step<T>(a, b, c, p, P, T(z[t]), xnext, xlast);
+            sink(p, xnext + dsh);
         }
     }
 }
@@ -346,15 +354,45 @@ __device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t
     draw_mode_chain_to<T>(m, j, sg, key0, key1, dsh, [&](int p, T v) { qs[qidx(j, p, rs)] = v; });
 }
 
-// Phase A on the sampling path of the chunk form: the G threads of one sample (lanes gmask)
-// each draw the modes j = g, g + G, ...; returns the source surface.
+// Phase A on the sampling path of the chunk form, by the G threads of one sample (lanes gmask),
+// in two passes so that the Philox / Box-Muller work is spread evenly when G does not divide N:
+// the N ceil(P/4) counters' normals are written to the sample's buffer, then the modes
+// j = g, g + G, ... are back-substituted in place (the same steps as draw_mode_chain_to, so the
+// same bits).  Returns the source surface.
 template <typename T>
 __device__ int draw_sample_smem(const pbr_model& m, T* qs, int rs, int64_t sidx, uint64_t offset,
                                 uint32_t key0, uint32_t key1, int g, int G, unsigned gmask) {
     const uint64_t sg = offset + static_cast<uint64_t>(sidx);
+    const int N = m.N, P = m.P, CP = (P + 3) >> 2;
+    const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
+    for (int u = g; u < N * CP; u += G) {
+        const int j = u / CP, p4 = u - j * CP;
+        const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(u), lo, hi, 0u}, key0, key1);
+        float z[4];
+        box_muller(r.x, r.y, z[0], z[1]);
+        box_muller(r.z, r.w, z[2], z[3]);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int p = 4 * p4 + t;
+            if (p < P) qs[qidx(j, p, rs)] = T(z[t]);
+        }
+    }
     const int src = draw_source<T>(m, sg, key0, key1);
-    const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * m.N;
-    for (int j = g; j < m.N; j += G) draw_mode_chain<T>(m, j, sg, key0, key1, dsrc[j], qs, rs);
+    const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * N;
+    __syncwarp(gmask);
+    for (int j = g; j < N; j += G) {
+        const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
+        const T* b = a + static_cast<int64_t>(N) * P;
+        const T* c = b + static_cast<int64_t>(N) * P;
+        const T dsh = dsrc[j];
+        T* qj = qs + j * rs;
+        T xnext = T(0), xlast = T(0);
+        for (int p = P - 1; p >= 0; --p) {
+            T* slot = qj + p + (p >> 5);
+            chain_step<T>(a, b, c, p, P, *slot, xnext, xlast);
+            *slot = xnext + dsh;
+        }
+    }
     __syncwarp(gmask);
     return src;
 }
