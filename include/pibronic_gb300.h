@@ -377,13 +377,13 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
  * split, three MMAs per K step, FP32 accumulation in TMEM).  K is laid out in quads of four
  * columns (d, e0..e0+3) over the bead row's slots s = [q_0..q_{N-1}, 0 up to NA = N rounded up to
  * 4, 1, 0, 0, 0]: quads (d < N, e0 = 0, 4, .. <= d) hold the pairs e <= d, quads (NA, j0) the
- * linear terms, quad (NA, NA) the energies, quads (NA + 1, NA) pad to a multiple of 16.
+ * linear terms, quad (NA, NA) the energies, quads (NA + 1, NA) pad to a multiple of 32.
  * pbr_tc_potential_dims gives the padded K extent n2p and the column count a2p (A(A+1)/2 rounded up
  * to 16).  pbr_tc_pack_potential turns vib_qq [N(N+1)/2][A(A+1)/2], vib_l [N][A(A+1)/2] and vib_e
  * [A(A+1)/2] (FP32 or FP64 as precision says; vib_l and vib_e nullable = zero) into b_packed
- * (pbr_tc_potential_packed_floats(N, A) = 2 * mp * n2p floats, mp = a2p rounded up to 128 (the
- * MMA's M), 16-byte aligned): per stage of 16 K columns, the TF32 hi part then the lo part, each
- * mp rows x 4 cores of 4 columns, core (row r, core c) at ((r/8)*4 + c)*8 + r%8 in 16-byte units.
+ * (pbr_tc_potential_packed_floats(N, A) = 2 * a2p * n2p floats, 16-byte aligned): per stage of 32
+ * K columns, the TF32 hi part then the lo part, each a2p rows x 8 cores of 4 columns, core (row r,
+ * core c) at ((r/8)*8 + c)*8 + r%8 in 16-byte units.
  * pbr_tc_potential writes vq [X * P][a2p] (FP32; row sample * P + bead, column pair_index(b, c))
  * from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in pbr_tc_gemm.  Replaces
  * pimc.py:1145-1150 (V of diagonalize_coupling_matrix).

