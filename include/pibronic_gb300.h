@@ -334,10 +334,11 @@ int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64
 int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, const float* rt,
                             const pbr_flow_save* save, float* g_o, float* g_z2, float* g_z1, void* stream);
 
-/* C [M][N] = beta C + sum_x A[x][M] B[x][N] (C is not read when beta == 0), split over the batch
- * and reduced in a fixed order; scratch holds pbr_gemm_tn_scratch(X, M, N) floats. */
+/* C [M][N] = beta C + sum_x A[x][M] B[x][N] (C is not read when beta == 0) and, when colsum is
+ * not NULL, colsum [N] = sum_x B[x][N] (the bias gradient that shares the B operand), split over
+ * the batch and reduced in a fixed order; scratch holds pbr_gemm_tn_scratch(X, M, N) floats. */
 int pbr_gemm_tn_acc(const float* A, const float* B, int64_t X, int32_t M, int32_t N, float beta, float* C,
-                    float* scratch, void* stream);
+                    float* colsum, float* scratch, void* stream);
 int64_t pbr_gemm_tn_scratch(int64_t X, int32_t M, int32_t N);
 
 /* out [N] = column sums of B [X][N]. */

@@ -105,7 +105,7 @@ def _declare(lib):
                                              C.POINTER(PbrFlowSave), vp]),
         "pbr_flow_layer_backward": (C.c_int, [C.POINTER(PbrFlowLayer), i64, vp, vp,
                                               C.POINTER(PbrFlowSave), vp, vp, vp, vp]),
-        "pbr_gemm_tn_acc": (C.c_int, [vp, vp, i64, i32, i32, C.c_float, vp, vp, vp]),
+        "pbr_gemm_tn_acc": (C.c_int, [vp, vp, i64, i32, i32, C.c_float, vp, vp, vp, vp]),
         "pbr_gemm_tn_scratch": (i64, [i64, i32, i32]),
         "pbr_colsum": (C.c_int, [vp, i64, i32, vp, vp]),
         "pbr_flow_base": (C.c_int, [vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),

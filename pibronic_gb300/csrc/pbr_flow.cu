@@ -702,10 +702,14 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
 constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
 constexpr int kGemmRowsPerSplit = 256;
 __global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B,
-                                                       int64_t X, int M, int N, int64_t chunk,
+                                                       int64_t X, int M, int N, int64_t chunk, int with_colsum,
                                                        float* __restrict__ part) {
     __shared__ __align__(16) float sa[kGBK][kGBM + kGPad];
     __shared__ __align__(16) float sb[kGBK][kGBN + kGPad];
+    // column sums of B ride along in the first row of blocks: thread (tx, ty) adds rows 2 ty and
+    // 2 ty + 1 of each staged tile for its four columns; the 16 partials are added in ty order
+    const bool colsum = with_colsum && blockIdx.x == 0;
+    float bs[4] = {0.f, 0.f, 0.f, 0.f};
     const int tm = blockIdx.x * kGBM, tn = blockIdx.y * kGBN, split = blockIdx.z;
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;       // 16 x 16 threads, 4 x 4 outputs each
     float acc[4][4];
@@ -722,6 +726,13 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__
             sb[r][c] = (xx < x1 && tn + c < N) ? B[xx * N + tn + c] : 0.f;
         }
         __syncthreads();
+        if (colsum) {
+#pragma unroll
+            for (int kk = 0; kk < 2; ++kk) {
+                const float4 v = *reinterpret_cast<const float4*>(&sb[2 * ty + kk][tx * 4]);
+                bs[0] += v.x; bs[1] += v.y; bs[2] += v.z; bs[3] += v.w;
+            }
+        }
 #pragma unroll 8
         for (int k = 0; k < kGBK; ++k) {
             const float4 a = *reinterpret_cast<const float4*>(&sa[k][ty * 4]);
@@ -734,6 +745,7 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__
         }
         __syncthreads();
     }
+    // partials: [split][M + 1][N], row M = the column sums
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int m = tm + ty * 4 + i;
@@ -741,17 +753,34 @@ __global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int n = tn + tx * 4 + j;
-            if (n < N) part[(static_cast<int64_t>(split) * M + m) * N + n] = acc[i][j];
+            if (n < N) part[(static_cast<int64_t>(split) * (M + 1) + m) * N + n] = acc[i][j];
+        }
+    }
+    if (colsum) {                                  // block-uniform
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sa[ty][tx * 4 + j] = bs[j];    // sa is free after the last tile
+        __syncthreads();
+        if (ty == 0) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                float t = 0.f;
+                for (int r = 0; r < 16; ++r) t += sa[r][tx * 4 + j];
+                const int n = tn + tx * 4 + j;
+                if (n < N) part[(static_cast<int64_t>(split) * (M + 1) + M) * N + n] = t;
+            }
         }
     }
 }
 
-__global__ void gemm_tn_reduce(const float* __restrict__ part, int splits, int MN, float beta,
-                               float* __restrict__ C) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < MN; i += gridDim.x * blockDim.x) {
+// partials [splits][M + 1][N] added in split order: rows < M into C, row M into colsum (if any)
+__global__ void gemm_tn_reduce(const float* __restrict__ part, int splits, int M, int N, float beta,
+                               float* __restrict__ C, float* __restrict__ colsum) {
+    const int MN = M * N, total = colsum ? MN + N : MN;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         float acc = 0.f;
-        for (int s = 0; s < splits; ++s) acc += part[static_cast<int64_t>(s) * MN + i];
-        C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
+        for (int s = 0; s < splits; ++s) acc += part[static_cast<int64_t>(s) * (MN + N) + i];
+        if (i < MN) C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
+        else colsum[i - MN] = acc;
     }
 }
 
@@ -1000,19 +1029,19 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
 int64_t pbr_gemm_tn_scratch(int64_t X, int32_t M, int32_t N) {
     const int64_t s = X / kGemmRowsPerSplit;
     const int64_t splits = s < 1 ? 1 : (s < 64 ? s : 64);
-    return splits * static_cast<int64_t>(M) * N;
+    return splits * (static_cast<int64_t>(M) + 1) * N;
 }
 
 int pbr_gemm_tn_acc(const float* A, const float* B, int64_t X, int32_t M, int32_t N, float beta, float* C,
-                    float* scratch, void* stream) {
+                    float* colsum, float* scratch, void* stream) {
     if (!A || !B || !C || !scratch || X < 1 || M < 1 || N < 1) return PBR_ERR_ARG;
-    const int64_t splits = pbr_gemm_tn_scratch(X, M, N) / (static_cast<int64_t>(M) * N);
+    const int64_t splits = pbr_gemm_tn_scratch(X, M, N) / ((static_cast<int64_t>(M) + 1) * N);
     const int64_t chunk = (X + splits - 1) / splits;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, static_cast<unsigned>(splits));
-    gemm_tn_partial<<<grid, 256, 0, st>>>(A, B, X, M, N, chunk, scratch);
-    gemm_tn_reduce<<<grid_for(static_cast<int64_t>(M) * N, 256), 256, 0, st>>>(scratch, static_cast<int>(splits),
-                                                                               M * N, beta, C);
+    gemm_tn_partial<<<grid, 256, 0, st>>>(A, B, X, M, N, chunk, colsum ? 1 : 0, scratch);
+    gemm_tn_reduce<<<grid_for((static_cast<int64_t>(M) + 1) * N, 256), 256, 0, st>>>(
+        scratch, static_cast<int>(splits), M, N, beta, C, colsum);
     return status();
 }
 

@@ -67,22 +67,40 @@ class FlowProposal:
         rng = np.random.default_rng(seed)
         idx = np.arange(self.D)
         self.idx = []
-        self.params = []
+        init = []
         for l in range(layers):
             a, b = (idx[0::2], idx[1::2]) if l % 2 == 0 else (idx[1::2], idx[0::2])
             I, J = len(a), len(b)
-            p = {
+            init.append({
                 "W1": rng.normal(0, 1 / math.sqrt(I), (I, hidden)), "b1": np.zeros(hidden),
                 "W2": rng.normal(0, 1 / math.sqrt(hidden), (hidden, hidden)), "b2": np.zeros(hidden),
                 "W3": rng.normal(0, init_scale / math.sqrt(hidden), (hidden, 2 * J)), "b3": np.zeros(2 * J),
-            }
-            self.params.append({k: torch.as_tensor(v, dtype=torch.float32, device=dev).contiguous()
-                                for k, v in p.items()})
+            })
             self.idx.append((torch.as_tensor(a, dtype=torch.int32, device=dev),
                              torch.as_tensor(b, dtype=torch.int32, device=dev)))
-        self.nu = torch.zeros(A, dtype=torch.float32, device=dev)
+        # every parameter (and nu) is a view into one flat FP32 buffer, the gradients into a second
+        # one of the same layout: the Adam update is a single launch; segments start on 16 bytes
+        self._segs, n = [], 0
+        for p in init:
+            seg = {}
+            for k, v in p.items():
+                seg[k] = (n, v.shape)
+                n += (v.size + 3) // 4 * 4
+            self._segs.append(seg)
+        self._nu_off = n
+        n += (A + 3) // 4 * 4
+        self._flat = torch.zeros(n, dtype=torch.float32, device=dev)
+        self._gflat = torch.zeros_like(self._flat)
+        self.params = [self._views(self._flat, l) for l in range(layers)]
+        for p, v in zip(self.params, init):
+            for k in p:
+                p[k].copy_(torch.as_tensor(v[k], dtype=torch.float32))
+        self.nu = self._flat[self._nu_off:self._nu_off + A]
         self._adam = None
         self.step_count = 0
+
+    def _views(self, flat, l):
+        return {k: flat[o:o + int(np.prod(shp))].view(*shp) for k, (o, shp) in self._segs[l].items()}
 
     # ------------------------------------------------------------------------------------------
     def layer_struct(self, l):
@@ -230,7 +248,8 @@ class FlowProposal:
     def gradients(self, y, r):
         """Loss and gradients of one minibatch: inverse pass with saved activations, base loss,
         back-propagation through the layers, weight-gradient GEMMs and bias sums.  Returns
-        (loss, [per-layer dict of gradients], gradient of nu)."""
+        (loss, [per-layer dict of gradients], gradient of nu); the gradients are views into the
+        flat gradient buffer, overwritten by the next call."""
         torch = _native.require_cuda()
         lib = _lib()
         p = _native.ptr
@@ -254,18 +273,18 @@ class FlowProposal:
             sv = self._saves[l]
             _native.check(lib.pbr_flow_layer_backward(st, B, p(gy), p(rt), sv.struct, p(g_o),
                                                       p(self._g_z2), p(self._g_z1), sh), "flow backward")
-            g = {k: torch.empty_like(v) for k, v in self.params[l].items()}
-            for (A_, B_, M, N, key) in ((sv.h2, g_o, self.H, 2 * J, "W3"),
-                                        (sv.h1, self._g_z2, self.H, self.H, "W2"),
-                                        (sv.ya, self._g_z1, I, self.H, "W1")):
-                _native.check(lib.pbr_gemm_tn_acc(p(A_), p(B_), B, M, N, 0.0, p(g[key]), p(self._scratch), sh),
-                              "weight gradient")
-            for (B_, N, key) in ((g_o, 2 * J, "b3"), (self._g_z2, self.H, "b2"), (self._g_z1, self.H, "b1")):
-                _native.check(lib.pbr_colsum(p(B_), B, N, p(g[key]), sh), "bias gradient")
+            g = self._views(self._gflat, l)
+            # weight gradients, with the bias gradient (the column sums of the same B) alongside
+            for (A_, B_, M, N, key, bkey) in ((sv.h2, g_o, self.H, 2 * J, "W3", "b3"),
+                                              (sv.h1, self._g_z2, self.H, self.H, "W2", "b2"),
+                                              (sv.ya, self._g_z1, I, self.H, "W1", "b1")):
+                _native.check(lib.pbr_gemm_tn_acc(p(A_), p(B_), B, M, N, 0.0, p(g[key]), p(g[bkey]),
+                                                  p(self._scratch), sh), "weight gradient")
             grads[l] = g
         gsum = torch.empty(self.A, dtype=torch.float32, device=self.dev)
         _native.check(lib.pbr_colsum(p(rgam), B, self.A, p(gsum), sh), "nu gradient")
-        g_nu = -(gsum - torch.exp(lp) * rt.sum())
+        g_nu = self._gflat[self._nu_off:self._nu_off + self.A]
+        torch.neg(gsum - torch.exp(lp) * rt.sum(), out=g_nu)
         return lterm.sum(), grads, g_nu
 
     def train_step(self, y, r, lr):
@@ -275,24 +294,17 @@ class FlowProposal:
         return loss
 
     def _adam_step(self, grads, g_nu, lr):
+        """One Adam update of every parameter and nu: the gradients are already in the flat
+        gradient buffer (grads and g_nu are views into it)."""
         torch = _native.require_cuda()
         lib = _lib()
         p = _native.ptr
         if self._adam is None:
-            self._adam = [{k: (torch.zeros_like(v), torch.zeros_like(v)) for k, v in pp.items()}
-                          for pp in self.params]
-            self._adam_nu = (torch.zeros_like(self.nu), torch.zeros_like(self.nu))
+            self._adam = (torch.zeros_like(self._flat), torch.zeros_like(self._flat))
         self.step_count += 1
-        sh = _native.stream_handle()
-        for l, g in enumerate(grads):
-            for k, v in self.params[l].items():
-                m, s = self._adam[l][k]
-                _native.check(lib.pbr_adam(p(v), p(g[k]), p(m), p(s), v.numel(), lr, 0.9, 0.999, 1e-8,
-                                           self.step_count, sh), "adam")
-        m, s = self._adam_nu
-        g_nu = g_nu.contiguous()
-        _native.check(lib.pbr_adam(p(self.nu), p(g_nu), p(m), p(s), self.nu.numel(), lr, 0.9, 0.999, 1e-8,
-                                   self.step_count, sh), "adam")
+        m, s = self._adam
+        _native.check(lib.pbr_adam(p(self._flat), p(self._gflat), p(m), p(s), self._flat.numel(), lr, 0.9, 0.999,
+                                   1e-8, self.step_count, _native.stream_handle()), "adam")
 
 
 class _Save:
