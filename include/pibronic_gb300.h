@@ -356,9 +356,10 @@ int pbr_flow_base(const float* y0, const double* ld, int64_t X, int32_t D, int32
 int pbr_flow_weights(const double* lse_y, const double* U, const double* logdet, const double* log_scale_x,
                      int64_t X, double* s_q, void* stream);
 
-/* Adam step (bias-corrected with the 1-based step). */
+/* Adam step: *step (device int32) is incremented first and the update is bias-corrected with the
+ * new value, so the call can be replayed from a captured CUDA graph. */
 int pbr_adam(float* param, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
-             float beta2, float eps, int32_t step, void* stream);
+             float beta2, float eps, int32_t* step, void* stream);
 
 /*
  * 5th-generation tensor-core GEMM (tcgen05.mma into TMEM, operands staged in shared memory in the

@@ -110,7 +110,7 @@ def _declare(lib):
         "pbr_colsum": (C.c_int, [vp, i64, i32, vp, vp]),
         "pbr_flow_base": (C.c_int, [vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
         "pbr_flow_weights": (C.c_int, [vp, vp, vp, vp, i64, vp, vp]),
-        "pbr_adam": (C.c_int, [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp]),
+        "pbr_adam": (C.c_int, [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp]),
         "pbr_batch_blob_bytes": (i64, [i32]),
         "pbr_batch_pack": (C.c_int, [vp, vp, vp, vp, vp, i32, i32, i32, vp]),
         "pbr_sample_eval_batch": (C.c_int, [vp, vp, vp]),

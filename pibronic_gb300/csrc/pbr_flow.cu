@@ -25,11 +25,40 @@ constexpr float kKappa = 2.0f;
 
 __host__ __device__ inline int align_up_(int x, int a) { return (x + a - 1) / a * a; }
 
+// The launch helpers below cache what they ask the runtime (SM count, per-kernel residency), so a
+// repeated launch -- in particular one recorded into a CUDA graph -- issues nothing but the launch.
+// The caches assume one device per process (as the library does) and calls from one host thread.
 inline int sm_count() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return sms > 0 ? sms : 1;
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0, n = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms = n > 0 ? n : 1;
+    }
+    return sms;
+}
+
+// blocks of kern resident per SM with `threads` threads and `bytes` of dynamic shared memory
+// (the opt-in limit raised to the whole 227 KB once per kernel); 0 when it cannot run
+template <typename K>
+int resident_blocks(K kern, int threads, int bytes) {
+    struct Entry { const void* f; int threads, bytes, occ; };
+    static Entry cache[64];
+    static int n = 0;
+    const void* f = reinterpret_cast<const void*>(kern);
+    bool opted = false;
+    for (int i = 0; i < n; ++i) {
+        if (cache[i].f != f) continue;
+        opted = true;
+        if (cache[i].threads == threads && cache[i].bytes == bytes) return cache[i].occ;
+    }
+    if (!opted && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) != cudaSuccess)
+        return 0;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, bytes) != cudaSuccess) return 0;
+    if (n < 64) cache[n++] = Entry{f, threads, bytes, occ};
+    return occ;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -847,9 +876,13 @@ __global__ void flow_weights_kernel(const double* __restrict__ lse_y, const doub
         s_q[x] = exp(lse_y[x] - 0.5 * U[x] - logdet[x] - log_scale_x[x]);
 }
 
+__global__ void adam_count_kernel(int32_t* step) { *step += 1; }
+
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
                             float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps,
-                            float c1, float c2) {
+                            const int32_t* __restrict__ step) {
+    const float t = static_cast<float>(*step);
+    const float c1 = 1.f - powf(b1, t), c2 = 1.f - powf(b2, t);
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const float gi = g[i];
@@ -899,10 +932,8 @@ int tile_smem(const pbr_flow_layer* l, bool fwd) {
 // persistent grid: one block per resident slot, no more blocks than tiles; 0 when it cannot run
 template <typename K>
 int tile_grid(K kern, int bytes, int64_t X) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return 0;
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTileThreads, bytes) != cudaSuccess || occ < 1)
-        return 0;
+    const int occ = resident_blocks(kern, kTileThreads, bytes);
+    if (occ < 1) return 0;
     const int64_t tiles = (X + kTileS - 1) / kTileS;
     const int64_t cap = static_cast<int64_t>(sm_count()) * occ;
     return static_cast<int>(tiles < cap ? tiles : cap);
@@ -966,12 +997,8 @@ int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64
     const int bytes = layer_smem_fwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
     auto go = [&](auto kern) -> int {
-        if (bytes > 48 * 1024 &&
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
-            return PBR_ERR_UNSUPPORTED;
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kFlowWarps * 32, bytes) != cudaSuccess || occ < 1)
-            return PBR_ERR_UNSUPPORTED;
+        const int occ = resident_blocks(kern, kFlowWarps * 32, bytes);
+        if (occ < 1) return PBR_ERR_UNSUPPORTED;
         const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
         const int cap = sm_count() * occ;
         kern<<<static_cast<int>(blocks < cap ? blocks : cap), kFlowWarps * 32, bytes,
@@ -1006,12 +1033,8 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
     const int bytes = layer_smem_bwd(layer);
     if (bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
     auto go = [&](auto kern) -> int {
-        if (bytes > 48 * 1024 &&
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
-            return PBR_ERR_UNSUPPORTED;
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kFlowWarps * 32, bytes) != cudaSuccess || occ < 1)
-            return PBR_ERR_UNSUPPORTED;
+        const int occ = resident_blocks(kern, kFlowWarps * 32, bytes);
+        if (occ < 1) return PBR_ERR_UNSUPPORTED;
         const int64_t blocks = (X + kFlowWarps - 1) / kFlowWarps;
         const int cap = sm_count() * occ;
         kern<<<static_cast<int>(blocks < cap ? blocks : cap), kFlowWarps * 32, bytes,
@@ -1073,13 +1096,12 @@ int pbr_flow_weights(const double* lse_y, const double* U, const double* logdet,
 }
 
 int pbr_adam(float* param, const float* grad, float* m, float* v, int64_t n, float lr, float beta1,
-             float beta2, float eps, int32_t step, void* stream) {
-    if (!param || !grad || !m || !v || n < 0 || step < 1) return PBR_ERR_ARG;
+             float beta2, float eps, int32_t* step, void* stream) {
+    if (!param || !grad || !m || !v || !step || n < 0) return PBR_ERR_ARG;
     if (n == 0) return PBR_OK;
-    const float c1 = 1.f - powf(beta1, static_cast<float>(step));
-    const float c2 = 1.f - powf(beta2, static_cast<float>(step));
-    adam_kernel<<<grid_for(n, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(param, grad, m, v, n, lr,
-                                                                                  beta1, beta2, eps, c1, c2);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    adam_count_kernel<<<1, 1, 0, st>>>(step);
+    adam_kernel<<<grid_for(n, 256), 256, 0, st>>>(param, grad, m, v, n, lr, beta1, beta2, eps, step);
     return status();
 }
 

@@ -96,8 +96,9 @@ class FlowProposal:
             for k in p:
                 p[k].copy_(torch.as_tensor(v[k], dtype=torch.float32))
         self.nu = self._flat[self._nu_off:self._nu_off + A]
+        self._t_log_w = torch.as_tensor(self.log_w, dtype=torch.float32, device=dev)
         self._adam = None
-        self.step_count = 0
+        self._step = torch.zeros(1, dtype=torch.int32, device=dev)       # Adam's step count
 
     def _views(self, flat, l):
         return {k: flat[o:o + int(np.prod(shp))].view(*shp) for k, (o, shp) in self._segs[l].items()}
@@ -114,7 +115,7 @@ class FlowProposal:
 
     def log_pi(self):
         torch = _native.require_cuda()
-        z = torch.as_tensor(self.log_w, dtype=torch.float32, device=self.dev) + self.nu
+        z = self._t_log_w + self.nu
         return z - torch.logsumexp(z, dim=0)
 
     def params_host(self):
@@ -209,18 +210,27 @@ class FlowProposal:
         return res
 
     # ------------------------------------------------------------------------------------------
-    def train(self, y, r, epochs=4, batch=8192, lr=1e-3, seed=0, log=None):
-        """Adam on the weighted forward KL over the dataset (y [X, D] CUDA FP32, r [X] weights)."""
+    @property
+    def step_count(self):
+        return int(self._step.item())
+
+    def train(self, y, r, epochs=4, batch=8192, lr=1e-3, seed=0, log=None, graph=True):
+        """Adam on the weighted forward KL over the dataset (y [X, D] CUDA FP32, r [X] weights).
+        A step (minibatch gather, inverse pass, back-propagation, gradients, Adam) runs on fixed
+        buffers; with graph=True it is captured as a CUDA graph after its first, eager run and
+        replayed for every further minibatch (the step is launch-bound: some 60 launches)."""
         torch = _native.require_cuda()
         X = y.shape[0]
         gen = torch.Generator(device="cpu").manual_seed(seed)
         hist = []
+        step = None
         for ep in range(epochs):
             perm = torch.randperm(X, generator=gen).to(self.dev)
             tot = torch.zeros((), dtype=torch.float64, device=self.dev)
             for b0 in range(0, X - batch + 1, batch):
-                idx = perm[b0:b0 + batch]
-                tot += self.train_step(y[idx].contiguous(), r[idx].contiguous(), lr)
+                if step is None:
+                    step = _TrainStep(self, y, r, batch, lr, graph)
+                tot += step(perm[b0:b0 + batch])
             hist.append(float(tot.item()) / max(1, X // batch))
             if log:
                 log(f"epoch {ep}: mean batch loss {hist[-1]:.6f}")
@@ -301,10 +311,43 @@ class FlowProposal:
         p = _native.ptr
         if self._adam is None:
             self._adam = (torch.zeros_like(self._flat), torch.zeros_like(self._flat))
-        self.step_count += 1
         m, s = self._adam
         _native.check(lib.pbr_adam(p(self._flat), p(self._gflat), p(m), p(s), self._flat.numel(), lr, 0.9, 0.999,
-                                   1e-8, self.step_count, _native.stream_handle()), "adam")
+                                   1e-8, p(self._step), _native.stream_handle()), "adam")
+
+
+class _TrainStep:
+    """One training step on fixed buffers (minibatch indices in, batch loss out); after its first
+    eager run it is captured as a CUDA graph (graph=True) and replayed."""
+
+    def __init__(self, fl, y, r, batch, lr, graph):
+        torch = _native.require_cuda()
+        self.fl, self.y, self.r, self.lr, self.want_graph = fl, y, r, lr, graph
+        self.idx = torch.empty(batch, dtype=torch.int64, device=fl.dev)
+        self.yb = torch.empty((batch,) + tuple(y.shape[1:]), dtype=y.dtype, device=fl.dev)
+        self.rb = torch.empty(batch, dtype=r.dtype, device=fl.dev)
+        self.loss = torch.zeros((), dtype=torch.float64, device=fl.dev)
+        self.graph = None
+
+    def _body(self):
+        torch = _native.require_cuda()
+        torch.index_select(self.y, 0, self.idx, out=self.yb)
+        torch.index_select(self.r, 0, self.idx, out=self.rb)
+        self.loss.copy_(self.fl.train_step(self.yb, self.rb, self.lr))
+
+    def __call__(self, idx):
+        torch = _native.require_cuda()
+        self.idx.copy_(idx)
+        if self.graph is not None:
+            self.graph.replay()
+            return self.loss
+        self._body()
+        if self.want_graph:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._body()
+            self.graph = g
+        return self.loss
 
 
 class _Save:
