@@ -413,6 +413,15 @@ def _timed(torch, fn):
     return r, time.perf_counter() - t0
 
 
+def _warm_training(torch, FlowProposal, prepared, plan, nsel, y, r):
+    """Two training steps of a throwaway proposal of the same shapes: on a fresh box the first use
+    of some PyTorch kernels compiles them (seconds), which would otherwise land in train_s."""
+    n = min(y.shape[0], 2 * 16384)
+    warm = FlowProposal(prepared, plan, nsel=nsel, layers=8, hidden=128, seed=1)
+    warm.train(y[:n].contiguous(), r[:n].contiguous(), epochs=1, batch=min(16384, n), lr=1e-3)
+    torch.cuda.synchronize()
+
+
 def learned_leg(args):
     """The learned-proposal configuration: plain rho vs the affine-coupling flow trained on 2e6 of
     rho's own weighted samples plus one round on its own samples; ESS/s includes the flow's
@@ -447,6 +456,7 @@ def learned_leg(args):
             ys.append(y)
             rs.append(pl["s_g"] / pl["s_rho"])
             del pl["q"]
+        _warm_training(torch, FlowProposal, data.prepared, data.plan, 3, ys[0], rs[0])
         _, t_train = _timed(torch, lambda: fl.train(torch.cat(ys), torch.cat(rs), epochs=6, batch=16384, lr=1e-3))
         first = fl.sample_and_evaluate(X, seed=7, keep=True)
         _, t2 = _timed(torch, lambda: fl.train(first["y"], first["s_g"] / first["s_q"], epochs=6, batch=16384,
@@ -565,6 +575,7 @@ def large_leg(args):
         y, _ = fl.prepare(plain["q"])
         r = plain["s_g"] / plain["s_rho"]
         del plain["q"]
+        _warm_training(torch, FlowProposal, data.prepared, plan, 2, y, r)
         _, t_train = _timed(torch, lambda: fl.train(y, r, epochs=6, batch=16384, lr=1e-3))
         del y
         fl.sample_and_evaluate(1000, seed=5)

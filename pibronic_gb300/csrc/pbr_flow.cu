@@ -430,11 +430,35 @@ struct TileDims {
     __host__ __device__ TileDims(int I, int J, int H, int HB)
         : I4(align_up_(I, 4)), Hp(align_up_(H, 64 * HB)), Op(align_up_(2 * J, 64)), Ip(align_up_(I, 64)),
           ldya(align_up_(align_up_(I, 4), 8) + 4), ldh(align_up_(H, 64 * HB) + 4), ldo(align_up_(2 * J, 64) + 4) {}
-    __host__ __device__ int fwd_floats() const {
-        return I4 * Hp + Hp * Hp + Hp * Op + 2 * Hp + Op + kTileS * (ldya + ldh);
+    // + the two index lists (int32) at the end
+    __host__ __device__ int fwd_floats(int I, int J) const {
+        return I4 * Hp + Hp * Hp + Hp * Op + 2 * Hp + Op + kTileS * (ldya + ldh) + align_up_(I + J, 4);
     }
-    __host__ __device__ int bwd_floats() const { return Op * Hp + Hp * Hp + Hp * Ip + kTileS * (ldo + ldh); }
+    __host__ __device__ int bwd_floats(int I, int J) const {
+        return Op * Hp + Hp * Hp + Hp * Ip + kTileS * (ldo + ldh) + align_up_(I + J, 4);
+    }
 };
+
+// store(i, load(i)) for i < n over the block with eight independent loads in flight per thread
+// before their stores (a plain loop keeps one global load outstanding per thread, and the
+// weight preload of a launch is then bound by memory latency)
+template <typename L, typename S>
+__device__ __forceinline__ void block_copy(int n, L&& load, S&& store) {
+    constexpr int U = 8;
+    for (int b = threadIdx.x; b < n; b += U * blockDim.x) {
+        float v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = b + u * blockDim.x;
+            v[u] = i < n ? load(i) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = b + u * blockDim.x;
+            if (i < n) store(i, v[u]);
+        }
+    }
+}
 
 __device__ __forceinline__ float f4c(const float4& v, int i) {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
@@ -500,36 +524,30 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_kernel(const Layer
     float* bb3 = bb2 + Hp;                // [Op], interleaved like w3
     float* ya = bb3 + Op;                 // [64][ldya]
     float* hs = ya + kTileS * ldya;       // [64][ldh]: h1, then h2
-    for (int i = threadIdx.x; i < I4 * Hp; i += blockDim.x) {
-        const int k = i / Hp, c = i - k * Hp;
-        w1[i] = (k < I && c < H) ? L.W1[k * H + c] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Hp * Hp; i += blockDim.x) {
-        const int k = i / Hp, c = i - k * Hp;
-        w2[i] = (k < H && c < H) ? L.W2[k * H + c] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Hp * Op; i += blockDim.x) {
-        const int k = i / Op, c = i - k * Op, j = c >> 1;
-        w3[i] = (k < H && j < J) ? L.W3[k * 2 * J + ((c & 1) ? J + j : j)] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Hp; i += blockDim.x) {
-        bb1[i] = i < H ? L.b1[i] : 0.f;
-        bb2[i] = i < H ? L.b2[i] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Op; i += blockDim.x) {
-        const int j = i >> 1;
-        bb3[i] = j < J ? L.b3[(i & 1) ? J + j : j] : 0.f;
-    }
+    int* ia = reinterpret_cast<int*>(hs + kTileS * ldh);   // idx_a [I], idx_b [J]
+    int* ib = ia + I;
+    for (int i = threadIdx.x; i < I + J; i += blockDim.x) ia[i] = i < I ? L.idx_a[i] : L.idx_b[i - I];
+    block_copy(I4 * Hp, [&](int i) { const int k = i / Hp, c = i - k * Hp;
+                                     return (k < I && c < H) ? L.W1[k * H + c] : 0.f; },
+               [&](int i, float v) { w1[i] = v; });
+    block_copy(Hp * Hp, [&](int i) { const int k = i / Hp, c = i - k * Hp;
+                                     return (k < H && c < H) ? L.W2[k * H + c] : 0.f; },
+               [&](int i, float v) { w2[i] = v; });
+    block_copy(Hp * Op, [&](int i) { const int k = i / Op, c = i - k * Op, j = c >> 1;
+                                     return (k < H && j < J) ? L.W3[k * 2 * J + ((c & 1) ? J + j : j)] : 0.f; },
+               [&](int i, float v) { w3[i] = v; });
+    block_copy(2 * Hp, [&](int i) { return i < Hp ? (i < H ? L.b1[i] : 0.f) : (i - Hp < H ? L.b2[i - Hp] : 0.f); },
+               [&](int i, float v) { bb1[i] = v; });                 // bb1 and bb2 are adjacent
+    block_copy(Op, [&](int i) { const int j = i >> 1; return j < J ? L.b3[(i & 1) ? J + j : j] : 0.f; },
+               [&](int i, float v) { bb3[i] = v; });
     const int sg = threadIdx.x >> 4, cg = threadIdx.x & 15;
     const int64_t ntiles = (X + kTileS - 1) / kTileS;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t x0 = t * kTileS;
         __syncthreads();                  // weights loaded / the previous tile's readers are done
-        for (int i = threadIdx.x; i < kTileS * I4; i += blockDim.x) {
-            const int s = i / I4, c = i - s * I4;
-            const int64_t x = x0 + s;
-            ya[s * ldya + c] = (c < I && x < X) ? y[x * D + __ldg(L.idx_a + c)] : 0.f;
-        }
+        block_copy(kTileS * I4, [&](int i) { const int s = i / I4, c = i - s * I4; const int64_t x = x0 + s;
+                                             return (c < I && x < X) ? y[x * D + ia[c]] : 0.f; },
+                   [&](int i, float v) { const int s = i / I4; ya[s * ldya + (i - s * I4)] = v; });
         __syncthreads();
         if (sv.ya) {
             for (int i = threadIdx.x; i < kTileS * I; i += blockDim.x) {
@@ -587,7 +605,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_kernel(const Layer
                     if (j >= J) continue;
                     const float sv_s = kKappa * tanhf(o[r][2 * pp] / kKappa);
                     const float to = o[r][2 * pp + 1];
-                    const int bi = __ldg(L.idx_b + j);
+                    const int bi = ib[j];
                     const float yb = y[x * D + bi];
                     const float out = (dir > 0) ? fmaf(yb, __expf(sv_s), to) : (yb - to) * __expf(-sv_s);
                     y[x * D + bi] = out;
@@ -629,18 +647,20 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
     float* w1t = w2t + Hp * Hp;           // [Hp][Ip] = W1^T
     float* go = w1t + Hp * Ip;            // [64][ldo]
     float* gz = go + kTileS * ldo;        // [64][ldh]: gz2, then gz1
-    for (int i = threadIdx.x; i < Op * Hp; i += blockDim.x) {
-        const int c = i / Hp, h = i - c * Hp, j = c >> 1;
-        w3t[i] = (j < J && h < H) ? L.W3[h * O + ((c & 1) ? J + j : j)] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Hp * Hp; i += blockDim.x) {
-        const int m = i / Hp, h = i - m * Hp;
-        w2t[i] = (m < H && h < H) ? L.W2[h * H + m] : 0.f;
-    }
-    for (int i = threadIdx.x; i < Hp * Ip; i += blockDim.x) {
-        const int h = i / Ip, a = i - h * Ip;
-        w1t[i] = (h < H && a < I) ? L.W1[a * H + h] : 0.f;
-    }
+    int* ia = reinterpret_cast<int*>(gz + kTileS * ldh);   // idx_a [I], idx_b [J]
+    int* ib = ia + I;
+    for (int i = threadIdx.x; i < I + J; i += blockDim.x) ia[i] = i < I ? L.idx_a[i] : L.idx_b[i - I];
+    // transposed copies: written along the shared-memory rows (a store across them would hit one
+    // bank per warp), read across the source rows with eight loads in flight per thread
+    block_copy(Op * Hp, [&](int i) { const int c = i / Hp, h = i - c * Hp, j = c >> 1;
+                                     return (j < J && h < H) ? L.W3[h * O + ((c & 1) ? J + j : j)] : 0.f; },
+               [&](int i, float v) { w3t[i] = v; });
+    block_copy(Hp * Hp, [&](int i) { const int m = i / Hp, h = i - m * Hp;
+                                     return (m < H && h < H) ? L.W2[h * H + m] : 0.f; },
+               [&](int i, float v) { w2t[i] = v; });
+    block_copy(Hp * Ip, [&](int i) { const int h = i / Ip, a = i - h * Ip;
+                                     return (h < H && a < I) ? L.W1[a * H + h] : 0.f; },
+               [&](int i, float v) { w1t[i] = v; });
     const int sg = threadIdx.x >> 4, cg = threadIdx.x & 15;
     const int OH = Op >> 1;
     const int64_t ntiles = (X + kTileS - 1) / kTileS;
@@ -653,7 +673,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
             const int64_t x = x0 + s;
             float gos = 0.f, gt = 0.f;
             if (j < J && x < X) {
-                const int bi = __ldg(L.idx_b + j);
+                const int bi = ib[j];
                 const float sj = sv.s[x * J + j], yb = sv.yb[x * J + j];
                 const float gyb = gy[x * D + bi];
                 const float es = __expf(-sj);
@@ -717,7 +737,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
 #pragma unroll
                 for (int v = 0; v < 4; ++v) {
                     const int a = cb + 4 * cg + v;
-                    if (a < I) gy[x * D + __ldg(L.idx_a + a)] += o[r][v];
+                    if (a < I) gy[x * D + ia[a]] += o[r][v];
                 }
             }
         }
@@ -730,7 +750,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
 // splits' partials are added in split order by gemm_tn_reduce, so the result is deterministic.
 constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
 constexpr int kGemmRowsPerSplit = 256;
-__global__ void __launch_bounds__(256) gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B,
+__global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B,
                                                        int64_t X, int M, int N, int64_t chunk, int with_colsum,
                                                        float* __restrict__ part) {
     __shared__ __align__(16) float sa[kGBK][kGBM + kGPad];
@@ -925,7 +945,8 @@ bool layer_ok(const pbr_flow_layer* l) {
 int tile_smem(const pbr_flow_layer* l, bool fwd) {
     if (l->H > 128) return 0;
     const TileDims td(l->I, l->J, l->H, l->H > 64 ? 2 : 1);
-    const int64_t bytes = static_cast<int64_t>(sizeof(float)) * (fwd ? td.fwd_floats() : td.bwd_floats());
+    const int64_t bytes = static_cast<int64_t>(sizeof(float)) *
+                          (fwd ? td.fwd_floats(l->I, l->J) : td.bwd_floats(l->I, l->J));
     return bytes <= 227 * 1024 ? static_cast<int>(bytes) : 0;
 }
 
