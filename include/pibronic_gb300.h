@@ -146,7 +146,9 @@ int pbr_eval_q_tc(const pbr_model* model, const float* q, int64_t X, const pbr_o
  * shared memory, 0 = the maximum; models grouped by surface count and series order; grid_cap
  * limits the persistent grid, 0 = occupancy x SMs); the caller copies it to a device buffer of the
  * same size; pbr_sample_eval_batch launches one persistent row-team kernel per group, CTAs taking
- * the concatenated tiles round-robin.  All models need precision 32.  The launches can be captured
+ * the concatenated tiles round-robin, except that groups of up to 4 surfaces (whose models all
+ * leave the kernel form to the library or ask for register chunks) run one register-chunk launch
+ * per model, the faster form there.  All models need precision 32.  The launches can be captured
  * in a CUDA graph (the blob holds everything they read).
  */
 int64_t pbr_batch_blob_bytes(int32_t n_models);

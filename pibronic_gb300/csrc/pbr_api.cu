@@ -249,8 +249,11 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
 // ---- batched multi-model launch ------------------------------------------------------------
 namespace {
 constexpr int kBatchMaxGroups = 16;
+// chunked: the group's models run as one register-chunk launch each instead of the batched
+// row-team launch (up to 4 surfaces the chunk form is 2.2-3x faster per sample; the launches
+// are short enough to sit in the same CUDA graph)
 struct BatchGroup {
-    int32_t A, K, n_items, smem_bytes;
+    int32_t A, K, n_items, smem_bytes, chunked, pad;
     int64_t first_item, total_tiles;
 };
 struct BatchHeader {
@@ -280,6 +283,7 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
             const int first = n;
             int64_t tiles = 0;
             int smem = 0;
+            bool chunked = A <= 4;
             for (int i = 0; i < n_models; ++i) {
                 const pbr_model& m = models[i];
                 if (m.A != A || m.K != K) continue;
@@ -293,12 +297,14 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
                 it.tile_begin = tiles;
                 tiles += (X[i] + it.a.S - 1) / it.a.S;
                 smem = std::max(smem, team_smem(it.a, kSample));
+                chunked = chunked && (m.variant == 0 || m.variant == 1);   // a model asking for teams keeps them
                 ++n;
             }
             if (n > first) {
                 if (hdr->n_groups >= kBatchMaxGroups) return PBR_ERR_UNSUPPORTED;
                 BatchGroup& g = hdr->groups[hdr->n_groups++];
                 g.A = A; g.K = K; g.n_items = n - first; g.smem_bytes = smem;
+                g.chunked = chunked ? 1 : 0;
                 g.first_item = first; g.total_tiles = tiles;
             }
         }
@@ -313,10 +319,21 @@ int pbr_sample_eval_batch(const void* host_blob, const void* device_blob, void* 
     const auto* hdr = static_cast<const BatchHeader*>(host_blob);
     const auto* items = reinterpret_cast<const TeamBatchItem*>(
         static_cast<const char*>(device_blob) + sizeof(BatchHeader));
+    const auto* hitems = reinterpret_cast<const TeamBatchItem*>(hdr + 1);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     for (int gi = 0; gi < hdr->n_groups; ++gi) {
         const BatchGroup& g = hdr->groups[gi];
         if (g.total_tiles == 0) continue;
+        if (g.chunked) {
+            // one register-chunk launch per model, from the host copy of its arguments
+            for (int64_t i = g.first_item; i < g.first_item + g.n_items; ++i) {
+                const TeamArgs& a = hitems[i].a;
+                const uint64_t seed = static_cast<uint64_t>(a.key0) | (static_cast<uint64_t>(a.key1) << 32);
+                const int rc = run_fused(&a.m, kSample, nullptr, a.X, seed, a.offset, &a.out, stream);
+                if (rc != PBR_OK) return rc;
+            }
+            continue;
+        }
         const TeamBatchItem* gitems = items + g.first_item;
         int rc = PBR_ERR_UNSUPPORTED;
         switch (g.A) {
