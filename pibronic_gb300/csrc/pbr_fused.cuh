@@ -348,51 +348,64 @@ __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, ui
     }
 }
 
-template <typename T>
-__device__ void draw_mode_chain(const pbr_model& m, int j, uint64_t sg, uint32_t key0, uint32_t key1,
-                                T dsh, T* qs, int rs) {
-    draw_mode_chain_to<T>(m, j, sg, key0, key1, dsh, [&](int p, T v) { qs[qidx(j, p, rs)] = v; });
+
+// The sampler in two passes, for kernel forms whose threads share a tile of samples: first the
+// standard normals of every (sample, mode, group of 4 beads) counter -- the Philox / Box-Muller
+// work, spread evenly over the threads -- are written to the samples' mode-major buffers, then
+// each (sample, mode) chain is back-substituted in place.  The counters and the chain steps are
+// those of draw_mode_chain_to, so the bits are the same.
+//
+// normals of samples s < ns (global index sg0 + s) into qs + s * qstride, work items
+// u = u0, u0 + du, ... of the ns N ceil(P/4) counters
+template <typename T, bool kOneSample = false>
+__device__ __forceinline__ void fill_normals(const pbr_model& m, T* qs, int qstride, int rs, int ns, uint64_t sg0,
+                                             uint32_t key0, uint32_t key1, int u0, int du) {
+    const int N = m.N, P = m.P, CP = (P + 3) >> 2, per = N * CP;
+    for (int u = u0; u < ns * per; u += du) {
+        const int s = kOneSample ? 0 : u / per, rem = u - s * per;
+        const int j = rem / CP, p4 = rem - j * CP;
+        const uint64_t sg = sg0 + static_cast<uint64_t>(s);
+        const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(rem), static_cast<uint32_t>(sg),
+                                            static_cast<uint32_t>(sg >> 32), 0u}, key0, key1);
+        float z[4];
+        box_muller(r.x, r.y, z[0], z[1]);
+        box_muller(r.z, r.w, z[2], z[3]);
+        T* qsj = qs + static_cast<int64_t>(s) * qstride;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int p = 4 * p4 + t;
+            if (p < P) qsj[qidx(j, p, rs)] = T(z[t]);
+        }
+    }
 }
 
-// Phase A on the sampling path of the chunk form, by the G threads of one sample (lanes gmask),
-// in two passes so that the Philox / Box-Muller work is spread evenly when G does not divide N:
-// the N ceil(P/4) counters' normals are written to the sample's buffer, then the modes
-// j = g, g + G, ... are back-substituted in place (the same steps as draw_mode_chain_to, so the
-// same bits).  Returns the source surface.
+// mode j of one sample, in place: normals in, q = x + dsh out (qj = the mode's row, skewed layout)
+template <typename T>
+__device__ __forceinline__ void back_substitute(const pbr_model& m, int j, T dsh, T* qj) {
+    const int N = m.N, P = m.P;
+    const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
+    const T* b = a + static_cast<int64_t>(N) * P;
+    const T* c = b + static_cast<int64_t>(N) * P;
+    T xnext = T(0), xlast = T(0);
+    for (int p = P - 1; p >= 0; --p) {
+        T* slot = qj + p + (p >> 5);
+        chain_step<T>(a, b, c, p, P, *slot, xnext, xlast);
+        *slot = xnext + dsh;
+    }
+}
+
+// Phase A of the chunk form, by the G threads of one sample (lanes gmask); returns the source
+// surface.
 template <typename T>
 __device__ int draw_sample_smem(const pbr_model& m, T* qs, int rs, int64_t sidx, uint64_t offset,
                                 uint32_t key0, uint32_t key1, int g, int G, unsigned gmask) {
     const uint64_t sg = offset + static_cast<uint64_t>(sidx);
-    const int N = m.N, P = m.P, CP = (P + 3) >> 2;
-    const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
-    for (int u = g; u < N * CP; u += G) {
-        const int j = u / CP, p4 = u - j * CP;
-        const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(u), lo, hi, 0u}, key0, key1);
-        float z[4];
-        box_muller(r.x, r.y, z[0], z[1]);
-        box_muller(r.z, r.w, z[2], z[3]);
-#pragma unroll
-        for (int t = 0; t < 4; ++t) {
-            const int p = 4 * p4 + t;
-            if (p < P) qs[qidx(j, p, rs)] = T(z[t]);
-        }
-    }
+    const int N = m.N;
+    fill_normals<T, true>(m, qs, 0, rs, 1, sg, key0, key1, g, G);
     const int src = draw_source<T>(m, sg, key0, key1);
     const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * N;
     __syncwarp(gmask);
-    for (int j = g; j < N; j += G) {
-        const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
-        const T* b = a + static_cast<int64_t>(N) * P;
-        const T* c = b + static_cast<int64_t>(N) * P;
-        const T dsh = dsrc[j];
-        T* qj = qs + j * rs;
-        T xnext = T(0), xlast = T(0);
-        for (int p = P - 1; p >= 0; --p) {
-            T* slot = qj + p + (p >> 5);
-            chain_step<T>(a, b, c, p, P, *slot, xnext, xlast);
-            *slot = xnext + dsh;
-        }
-    }
+    for (int j = g; j < N; j += G) back_substitute<T>(m, j, dsrc[j], qs + j * rs);
     __syncwarp(gmask);
     return src;
 }

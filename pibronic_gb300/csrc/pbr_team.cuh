@@ -162,13 +162,14 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
             for (int s = tid; s < S; s += NT)
                 s_src[s] = (s < nvalid) ? draw_source<T>(m, args.offset + static_cast<uint64_t>(base + s),
                                                          args.key0, args.key1) : 0;
+            // the tile's normals over all threads, then one back-substitution chain per (sample, mode)
+            fill_normals<T>(m, s_q, args.qstride, rs, nvalid, args.offset + static_cast<uint64_t>(base),
+                            args.key0, args.key1, tid, NT);
             __syncthreads();
-            // one back-substitution chain per (sample, mode)
             for (int it = tid; it < nvalid * N; it += NT) {
                 const int s = it / N, j = it - s * N;
                 const T dsh = static_cast<const T*>(m.rho_d)[static_cast<int64_t>(s_src[s]) * N + j];
-                draw_mode_chain<T>(m, j, args.offset + static_cast<uint64_t>(base + s), args.key0,
-                                   args.key1, dsh, s_q + s * args.qstride, rs);
+                back_substitute<T>(m, j, dsh, s_q + s * args.qstride + j * rs);
             }
             __syncthreads();
             if (args.out.q_out || args.out.src_out) {
