@@ -248,7 +248,7 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
 
 // ---- batched multi-model launch ------------------------------------------------------------
 namespace {
-constexpr int kBatchMaxGroups = 16;
+constexpr int kBatchMaxGroups = 32;
 // chunked: the group's models run as one register-chunk launch each instead of the batched
 // row-team launch (up to 4 surfaces the chunk form is 2.2-3x faster per sample; the launches
 // are short enough to sit in the same CUDA graph)
@@ -277,9 +277,11 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->grid_cap = grid_cap;
     int n = 0;
-    // group by (A, K) in increasing A; within a group keep the caller's order
+    // group by (A, K) in increasing A, and at 5-6 surfaces by whether two tiles fit an SM (those
+    // models run the two-block build); within a group keep the caller's order
     for (int A = 1; A <= PBR_MAX_A; ++A)
-        for (int K = 0; K <= 4; K += 4) {
+        for (int K = 0; K <= 4; K += 4)
+        for (int cls = 0; cls < 2; ++cls) {
             const int first = n;
             int64_t tiles = 0;
             int smem = 0;
@@ -291,9 +293,13 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
                     m.N > PBR_MAX_N || m.P < 3 || m.P > PBR_MAX_P || X[i] < 0 || !outs[i].s_rho || !outs[i].s_g ||
                     (K > 0 && (!outs[i].s_gp || !outs[i].s_gm)) || !m.ring_chol || !m.src_cdf)
                     return PBR_ERR_ARG;
-                TeamBatchItem& it = items[n];
-                const int rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], budget, &it.a);
+                TeamArgs a;
+                const int rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], budget, &a);
                 if (rc != PBR_OK) return rc;
+                const bool two = (A == 5 || A == 6) && team_smem(a, kSample) <= kTeamTwoBlockSmem;
+                if ((cls == 0) != two) continue;
+                TeamBatchItem& it = items[n];
+                it.a = a;
                 it.tile_begin = tiles;
                 tiles += (X[i] + it.a.S - 1) / it.a.S;
                 smem = std::max(smem, team_smem(it.a, kSample));

@@ -578,8 +578,15 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     }
 }
 
-template <int A, int K, int QM, typename T>
-__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1)) pimc_team_kernel(const TeamArgs args) {
+// MB: the blocks per SM the registers are sized for.  Two up to 4 surfaces; from 5 on one, plus a
+// two-block build for 5 and 6 surfaces that the launcher picks when two tiles fit the shared memory
+// of an SM (measured: +24-29 % at P = 32-64; at 7-8 surfaces the 128-register build spills and loses
+// 10-13 %).
+template <int A> constexpr int team_min_blocks() { return A <= 4 ? 2 : 1; }
+constexpr int kTeamTwoBlockSmem = 113 * 1024;
+
+template <int A, int K, int QM, typename T, int MB = team_min_blocks<A>()>
+__global__ void __launch_bounds__(kTeamThreads, MB) pimc_team_kernel(const TeamArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
@@ -603,8 +610,8 @@ struct TeamBatchItem {
     int64_t tile_begin;       // first tile of this model in the launch
 };
 
-template <int A, int K>
-__global__ void __launch_bounds__(kTeamThreads, (A <= 4 ? 2 : 1))
+template <int A, int K, int MB = team_min_blocks<A>()>
+__global__ void __launch_bounds__(kTeamThreads, MB)
 pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int64_t total_tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);

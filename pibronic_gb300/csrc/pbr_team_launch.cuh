@@ -7,29 +7,38 @@
 
 namespace pbr {
 
-template <int A, int K, int QM, typename T>
-static int launch_team_one(const TeamArgs& args, cudaStream_t stream) {
-    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
-                        args.qstride, args.rl);
-    auto kern = pimc_team_kernel<A, K, QM, T>;
+// the two-block build applies at 5 and 6 surfaces in FP32 when two tiles fit an SM
+template <int A, typename T>
+constexpr bool team_two_block_build() { return (A == 5 || A == 6) && sizeof(T) == 4; }
+
+template <int A, int K, int QM, typename T, int MB>
+static int launch_team_kern(const TeamArgs& args, int smem_bytes, cudaStream_t stream) {
+    auto kern = pimc_team_kernel<A, K, QM, T, MB>;
     static int configured = 0;
-    if (plan.total_bytes > 48 * 1024 && plan.total_bytes > configured) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 plan.total_bytes) != cudaSuccess)
+    if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) != cudaSuccess)
             return PBR_ERR_UNSUPPORTED;
-        configured = plan.total_bytes;
+        configured = smem_bytes;
     }
     int dev = 0, sms = 0, occ = 0;
     PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
     PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTeamThreads,
-                                                                     plan.total_bytes));
+    PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTeamThreads, smem_bytes));
     if (occ < 1) return PBR_ERR_UNSUPPORTED;
     const int64_t need = (args.X + args.S - 1) / args.S;
     const int grid = static_cast<int>(std::min<int64_t>(need, static_cast<int64_t>(occ) * sms));
     if (grid <= 0) return PBR_OK;
-    kern<<<grid, kTeamThreads, plan.total_bytes, stream>>>(args);
+    kern<<<grid, kTeamThreads, smem_bytes, stream>>>(args);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+template <int A, int K, int QM, typename T>
+static int launch_team_one(const TeamArgs& args, cudaStream_t stream) {
+    const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
+                        args.qstride, args.rl);
+    if constexpr (team_two_block_build<A, T>())
+        if (plan.total_bytes <= kTeamTwoBlockSmem) return launch_team_kern<A, K, QM, T, 2>(args, plan.total_bytes, stream);
+    return launch_team_kern<A, K, QM, T, team_min_blocks<A>()>(args, plan.total_bytes, stream);
 }
 
 template <int A>
@@ -55,10 +64,10 @@ int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStrea
     return launch_team_one<A, 4, kQ64, double>(args, stream);
 }
 
-template <int A, int K>
-static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
-                                 int grid_cap, cudaStream_t stream) {
-    auto kern = pimc_team_batch_kernel<A, K>;
+template <int A, int K, int MB>
+static int launch_team_batch_kern(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
+                                  int grid_cap, cudaStream_t stream) {
+    auto kern = pimc_team_batch_kernel<A, K, MB>;
     if (smem_bytes > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) != cudaSuccess)
         return PBR_ERR_UNSUPPORTED;
@@ -72,6 +81,16 @@ static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_
     if (grid <= 0) return PBR_OK;
     kern<<<static_cast<int>(grid), kTeamThreads, smem_bytes, stream>>>(items, n_items, total_tiles);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+template <int A, int K>
+static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
+                                 int grid_cap, cudaStream_t stream) {
+    if constexpr (team_two_block_build<A, float>())
+        if (smem_bytes <= kTeamTwoBlockSmem)
+            return launch_team_batch_kern<A, K, 2>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
+    return launch_team_batch_kern<A, K, team_min_blocks<A>()>(items, n_items, total_tiles, smem_bytes, grid_cap,
+                                                              stream);
 }
 
 template <int A>
