@@ -16,6 +16,8 @@ int tc_quadratic_launch(const float*, int64_t, int, int, int, const void*, float
 int tc_pack_launch(const void*, const void*, const void*, int, int, int, void*, cudaStream_t);
 extern template int launch_wide<12>(int, const WideArgs&, cudaStream_t);   // pbr_wide_a12.cu
 extern template int launch_wide<16>(int, const WideArgs&, cudaStream_t);   // pbr_wide_a16.cu
+extern template int wide_resident<12>(int, const WideArgs&);
+extern template int wide_resident<16>(int, const WideArgs&);
 }
 
 namespace {
@@ -383,8 +385,8 @@ int64_t tc_fixed_bytes(const pbr_model& m) {
 }
 
 // The wide form's tile: up to 16 teams per sample, windows of up to 8 beads per team.
-int run_wide(const pbr_model& m, const float* q, const float* vq, int ld, int64_t X, const pbr_outputs* out,
-             cudaStream_t st) {
+pbr::WideArgs make_wide_args(const pbr_model& m, const float* q, const float* vq, int ld, int64_t X,
+                             const pbr_outputs* out) {
     using namespace pbr;
     WideArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -393,12 +395,26 @@ int run_wide(const pbr_model& m, const float* q, const float* vq, int ld, int64_
     a.vq = vq;
     a.vq_ld = ld;
     a.X = X;
-    a.out = *out;
+    if (out) a.out = *out;
     a.G = std::min(kWideTeams, m.P);
     a.C = (m.P + a.G - 1) / a.G;
     a.W = std::min(a.C, 8);
+    return a;
+}
+
+int run_wide(const pbr_model& m, const float* q, const float* vq, int ld, int64_t X, const pbr_outputs* out,
+             cudaStream_t st) {
+    using namespace pbr;
+    const WideArgs a = make_wide_args(m, q, vq, ld, X, out);
     if (m.A <= 12) return launch_wide<12>(m.K, a, st);
     return launch_wide<16>(m.K, a, st);
+}
+
+// samples the wide kernel evaluates in one wave (one per resident block); 0 when it cannot run
+int64_t wide_wave(const pbr_model& m, int ld) {
+    using namespace pbr;
+    const WideArgs a = make_wide_args(m, nullptr, nullptr, ld, 1, nullptr);
+    return m.A <= 12 ? wide_resident<12>(m.K, a) : wide_resident<16>(m.K, a);
 }
 
 int64_t tc_sample_bytes(const pbr_model& m) {
@@ -434,10 +450,17 @@ int run_tc(const pbr_model* model, const float* q_in, uint64_t seed, uint64_t of
     const bool wide = m.A > PBR_MAX_A;
     if (reinterpret_cast<uintptr_t>(scratch) % kScratchAlign) return PBR_ERR_ARG;
     const int64_t per = tc_sample_bytes(m);
-    const int64_t chunk = (scratch_bytes - tc_fixed_bytes(m) - 2 * kScratchAlign) / per;
+    int64_t chunk = (scratch_bytes - tc_fixed_bytes(m) - 2 * kScratchAlign) / per;
     if (chunk < 1) return PBR_ERR_CAPACITY;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int A2P = tc_quadratic_cols(m.A);
+    if (wide && chunk < X) {
+        // the wide kernel takes one sample per block: a chunk of whole waves leaves no block idle
+        // while others finish a last sample (455 samples on 304 resident blocks ran as 2 waves of
+        // which the second was half empty)
+        const int64_t wave = wide_wave(m, A2P);
+        if (wave > 0 && chunk >= wave) chunk = chunk / wave * wave;
+    }
     unsigned char* base = static_cast<unsigned char*>(scratch);
     void* bpack = base;
     float* qbuf = reinterpret_cast<float*>(base + tc_fixed_bytes(m));

@@ -504,8 +504,11 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
     __syncthreads();
 }
 
-template <int AP, int K>
-__global__ void __launch_bounds__(kWideThreads, AP <= 12 ? 2 : 1) pimc_wide_kernel(const WideArgs args) {
+// MB: blocks per SM the registers are sized for (two at AP = 12: 128 registers; one at AP = 16)
+template <int AP> constexpr int wide_min_blocks() { return AP <= 12 ? 2 : 1; }
+
+template <int AP, int K, int MB = wide_min_blocks<AP>()>
+__global__ void __launch_bounds__(kWideThreads, MB) pimc_wide_kernel(const WideArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float* sm = reinterpret_cast<float*>(smem_raw);
     const WidePlan plan(AP, K, args.m.N, args.G, args.W, args.vq_ld);
@@ -514,11 +517,12 @@ __global__ void __launch_bounds__(kWideThreads, AP <= 12 ? 2 : 1) pimc_wide_kern
     for (int64_t x = blockIdx.x; x < args.X; x += gridDim.x) wide_sample<AP, K>(args, sm, plan, x);
 }
 
-// Host launcher (one instantiation per padded width AP and series order K).
-template <int AP, int K>
-int launch_wide_one(const WideArgs& args, cudaStream_t stream) {
+// Host side (one instantiation per padded width AP and series order K).  A block evaluates one
+// sample at a time, so the caller sizes its chunks in whole waves of wide_resident() samples.
+template <int AP, int K, int MB>
+int wide_blocks_resident(const WideArgs& args, int* resident) {
     const WidePlan plan(AP, K, args.m.N, args.G, args.W, args.vq_ld);
-    auto kern = pimc_wide_kernel<AP, K>;
+    auto kern = pimc_wide_kernel<AP, K, MB>;
     if (plan.total_bytes > 227 * 1024) return PBR_ERR_UNSUPPORTED;
     static int configured = 0;
     if (plan.total_bytes > 48 * 1024 && plan.total_bytes > configured) {
@@ -531,15 +535,36 @@ int launch_wide_one(const WideArgs& args, cudaStream_t stream) {
     PBR_CUDA_CHECK_RET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     PBR_CUDA_CHECK_RET(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kWideThreads, plan.total_bytes));
     if (occ < 1) return PBR_ERR_UNSUPPORTED;
-    const int64_t grid = args.X < static_cast<int64_t>(occ) * sms ? args.X : static_cast<int64_t>(occ) * sms;
+    *resident = occ * sms;
+    return PBR_OK;
+}
+
+template <int AP, int K, int MB>
+int launch_wide_one(const WideArgs& args, cudaStream_t stream) {
+    int resident = 0;
+    const int rc = wide_blocks_resident<AP, K, MB>(args, &resident);
+    if (rc != PBR_OK) return rc;
+    const int64_t grid = args.X < resident ? args.X : resident;
     if (grid <= 0) return PBR_OK;
-    kern<<<static_cast<int>(grid), kWideThreads, plan.total_bytes, stream>>>(args);
+    const WidePlan plan(AP, K, args.m.N, args.G, args.W, args.vq_ld);
+    pimc_wide_kernel<AP, K, MB><<<static_cast<int>(grid), kWideThreads, plan.total_bytes, stream>>>(args);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 
 template <int AP>
 int launch_wide(int K, const WideArgs& args, cudaStream_t stream) {
-    return K == 0 ? launch_wide_one<AP, 0>(args, stream) : launch_wide_one<AP, 4>(args, stream);
+    constexpr int MB = wide_min_blocks<AP>();
+    return K == 0 ? launch_wide_one<AP, 0, MB>(args, stream) : launch_wide_one<AP, 4, MB>(args, stream);
+}
+
+// blocks launch_wide keeps resident (0 when it cannot run)
+template <int AP>
+int wide_resident(int K, const WideArgs& args) {
+    constexpr int MB = wide_min_blocks<AP>();
+    int resident = 0;
+    const int rc = K == 0 ? wide_blocks_resident<AP, 0, MB>(args, &resident)
+                          : wide_blocks_resident<AP, 4, MB>(args, &resident);
+    return rc == PBR_OK ? resident : 0;
 }
 
 }  // namespace pbr

@@ -3,4 +3,5 @@
 
 namespace pbr {
 template int launch_wide<16>(int, const WideArgs&, cudaStream_t);
+template int wide_resident<16>(int, const WideArgs&);
 }
