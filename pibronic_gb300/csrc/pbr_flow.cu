@@ -65,13 +65,17 @@ int resident_blocks(K kern, int threads, int bytes) {
 // prepare: y[x][j*nsel + s] = (sum_p B_ps (q_jp - c_j)) * inv_sigma[j*nsel + s],
 //          U[x] = sum_j (q_j - c_j)^T Lambda_j (q_j - c_j) - sum |y|^2
 // Lambda_j = 2 coth I - csch C evaluated as sum_p csch (dx)^2 + 2 tanh(tau w/2) x_p^2.
-// One warp per (sample); lanes over beads.
+// One warp per (sample); lanes over beads.  FP32 within a mode (the lanes' partial sums and their
+// shuffle reduction), FP64 only across modes: the FP64 pipe of this part runs at a small fraction
+// of the FP32 rate, and FP64 shuffles and products per mode made the kernel FP64-bound.
 // ---------------------------------------------------------------------------------------------
 __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int N, int P, int nsel,
                                     const double* __restrict__ center, const double* __restrict__ inv_sigma,
                                     const double* __restrict__ rho_csch, const double* __restrict__ rho_tanh2,
                                     float* __restrict__ y, double* __restrict__ U) {
-    extern __shared__ float basis[];            // [nsel][P] ring basis columns, FP32
+    extern __shared__ float basis[];            // [nsel][P] ring basis columns, then per mode (FP32):
+    float* s_isig = basis + nsel * P;           // inv_sigma [N][nsel]
+    float* s_mode = s_isig + N * nsel;          // [N][4]: center, csch, 2 tanh(tau w / 2), 0
     const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
     const double amp = sqrt(2.0 / P);
     for (int i = threadIdx.x; i < nsel * P; i += blockDim.x) {
@@ -84,16 +88,23 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
         }
         basis[i] = static_cast<float>(bv);
     }
+    for (int i = threadIdx.x; i < N * nsel; i += blockDim.x) s_isig[i] = static_cast<float>(inv_sigma[i]);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        s_mode[4 * j] = static_cast<float>(center[j]);
+        s_mode[4 * j + 1] = static_cast<float>(rho_csch[j]);
+        s_mode[4 * j + 2] = static_cast<float>(2.0 * rho_tanh2[j]);
+        s_mode[4 * j + 3] = 0.f;
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t gw = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
     const int64_t nw = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
     for (int64_t x = gw; x < X; x += nw) {
-        double quad_total = 0.0, ysq = 0.0;
+        double quad_total = 0.0;
+        float ysq = 0.0f;
         for (int j = 0; j < N; ++j) {
             const float* qj = q + (x * N + j) * static_cast<int64_t>(P);
-            const float c = static_cast<float>(center[j]);
-            const float ch = static_cast<float>(rho_csch[j]), th2 = static_cast<float>(2.0 * rho_tanh2[j]);
+            const float c = s_mode[4 * j], ch = s_mode[4 * j + 1], th2 = s_mode[4 * j + 2];
             float quad = 0.0f;
             float proj[8];
 #pragma unroll
@@ -107,23 +118,23 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
                 for (int s = 0; s < 8; ++s)
                     if (s < nsel) proj[s] = fmaf(basis[s * P + p], xp, proj[s]);
             }
-            double qd = static_cast<double>(quad);
 #pragma unroll
             for (int o = 16; o >= 1; o >>= 1) {
-                qd += __shfl_xor_sync(0xffffffffu, qd, o);
+                quad += __shfl_xor_sync(0xffffffffu, quad, o);
 #pragma unroll
-                for (int s = 0; s < 8; ++s) proj[s] += __shfl_xor_sync(0xffffffffu, proj[s], o);
+                for (int s = 0; s < 8; ++s)
+                    if (s < nsel) proj[s] += __shfl_xor_sync(0xffffffffu, proj[s], o);   // nsel is uniform
             }
-            quad_total += qd;
+            quad_total += static_cast<double>(quad);
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 if (s >= nsel) break;
-                const double v = static_cast<double>(proj[s]) * inv_sigma[j * nsel + s];
-                ysq += v * v;
-                if (lane == 0) y[x * static_cast<int64_t>(N * nsel) + j * nsel + s] = static_cast<float>(v);
+                const float v = proj[s] * s_isig[j * nsel + s];
+                ysq = fmaf(v, v, ysq);
+                if (lane == 0) y[x * static_cast<int64_t>(N * nsel) + j * nsel + s] = v;
             }
         }
-        if (lane == 0) U[x] = quad_total - ysq;
+        if (lane == 0) U[x] = quad_total - static_cast<double>(ysq);
     }
 }
 
@@ -131,7 +142,8 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
 __global__ void flow_apply_kernel(const float* __restrict__ q, const float* __restrict__ y,
                                   const float* __restrict__ yn, int64_t X, int N, int P, int nsel,
                                   const double* __restrict__ sigma, float* __restrict__ xo) {
-    extern __shared__ float basis[];            // [nsel][P]
+    extern __shared__ float basis[];            // [nsel][P], then sigma [N][nsel] in FP32
+    float* s_sig = basis + nsel * P;
     const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
     const double amp = sqrt(2.0 / P);
     for (int i = threadIdx.x; i < nsel * P; i += blockDim.x) {
@@ -144,19 +156,28 @@ __global__ void flow_apply_kernel(const float* __restrict__ q, const float* __re
         }
         basis[i] = static_cast<float>(bv);
     }
+    for (int i = threadIdx.x; i < N * nsel; i += blockDim.x) s_sig[i] = static_cast<float>(sigma[i]);
     __syncthreads();
-    const int64_t total = X * N * static_cast<int64_t>(P);
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int p = static_cast<int>(i % P);
-        const int64_t xj = i / P;
-        const int j = static_cast<int>(xj % N);
-        const int64_t x = xj / N;
-        float acc = q[i];
-        const int64_t y0 = x * static_cast<int64_t>(N * nsel) + j * nsel;
-        for (int s = 0; s < nsel; ++s)
-            acc = fmaf(basis[s * P + p] * static_cast<float>(sigma[j * nsel + s]), yn[y0 + s] - y[y0 + s], acc);
-        xo[i] = acc;
+    // a warp per (sample, mode) row: its nsel displacements once, lanes over the beads
+    const int lane = threadIdx.x & 31;
+    const int64_t rows = X * N;
+    const int64_t w0 = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t row = w0; row < rows; row += nw) {
+        const int j = static_cast<int>(row % N);
+        float dy[8];
+#pragma unroll
+        for (int s = 0; s < 8; ++s)
+            dy[s] = s < nsel ? s_sig[j * nsel + s] * (yn[row * nsel + s] - y[row * nsel + s]) : 0.f;
+        const float* qr = q + row * P;
+        float* xr = xo + row * P;
+        for (int p = lane; p < P; p += 32) {
+            float acc = qr[p];
+#pragma unroll
+            for (int s = 0; s < 8; ++s)
+                if (s < nsel) acc = fmaf(basis[s * P + p], dy[s], acc);
+            xr[p] = acc;
+        }
     }
 }
 
@@ -867,7 +888,8 @@ __global__ void flow_base_kernel(const float* __restrict__ y0, const double* __r
         }
         float den = 0.f;
         for (int a = 0; a < A; ++a) { e[a] = __expf(e[a] - mx); den += e[a]; }
-        const double lse = static_cast<double>(mx) + log(static_cast<double>(den));
+        // den is in [1, A]: its FP32 log is exact to ~1e-7 absolute, the scale of mx in FP64
+        const double lse = static_cast<double>(mx) + static_cast<double>(logf(den));
         const float w = rt ? rt[x] : 0.f;
         for (int a = 0; a < A; ++a) {
             e[a] /= den;
@@ -893,7 +915,7 @@ __global__ void flow_weights_kernel(const double* __restrict__ lse_y, const doub
                                     int64_t X, double* __restrict__ s_q) {
     for (int64_t x = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; x < X;
          x += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        s_q[x] = exp(lse_y[x] - 0.5 * U[x] - logdet[x] - log_scale_x[x]);
+        s_q[x] = pbr::exp_out_fp32(lse_y[x] - 0.5 * U[x] - logdet[x] - log_scale_x[x]);
 }
 
 __global__ void adam_count_kernel(int32_t* step) { *step += 1; }
@@ -977,8 +999,9 @@ int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t ns
         return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int threads = 128;
-    flow_prepare_kernel<<<grid_for(X * 32, threads), threads, nsel * P * sizeof(float),
-                          static_cast<cudaStream_t>(stream)>>>(
+    const int bytes = static_cast<int>(sizeof(float)) * (nsel * P + N * nsel + 4 * N);
+    if (resident_blocks(flow_prepare_kernel, threads, bytes) < 1) return PBR_ERR_UNSUPPORTED;
+    flow_prepare_kernel<<<grid_for(X * 32, threads), threads, bytes, static_cast<cudaStream_t>(stream)>>>(
         q, X, N, P, nsel, center, inv_sigma, rho_csch, rho_tanh2, y, U);
     return status();
 }
@@ -989,8 +1012,9 @@ int pbr_flow_apply(const float* q, const float* y, const float* y_new, int64_t X
         nsel > 1 + 2 * ((P - 1) / 2))
         return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
-    flow_apply_kernel<<<grid_for(X * N * P, 256), 256, nsel * P * sizeof(float),
-                        static_cast<cudaStream_t>(stream)>>>(
+    const int bytes = static_cast<int>(sizeof(float)) * (nsel * P + N * nsel);
+    if (resident_blocks(flow_apply_kernel, 256, bytes) < 1) return PBR_ERR_UNSUPPORTED;
+    flow_apply_kernel<<<grid_for(X * N * 32, 256), 256, bytes, static_cast<cudaStream_t>(stream)>>>(
         q, y, y_new, X, N, P, nsel, sigma, x);
     return status();
 }
