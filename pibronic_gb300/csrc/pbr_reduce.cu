@@ -1,9 +1,9 @@
 // pbr_reduce.cu -- FP64 device reductions of the per-sample outputs into estimator moments.
 //
-// Each thread keeps Welford (count, mean, M2) triples over a strided range; triples are merged
-// with Chan's pairwise formula, first across the warp by shuffles, then across the block in
-// shared memory, then across blocks by a single-block second pass, always in the same order,
-// so results are bitwise reproducible for a given X.
+// Each thread keeps shifted sums over a strided range and turns them into (count, mean, M2)
+// triples; triples are merged with Chan's pairwise formula, first across the warp by shuffles,
+// then across the block in shared memory, then across blocks by a single-block second pass,
+// always in the same order, so results are bitwise reproducible for a given X.
 #include "pbr_common.cuh"
 
 namespace {
@@ -13,13 +13,6 @@ constexpr int64_t kPerBlock = 4096;
 constexpr int kMaxBlocks = 4096;
 
 struct Moments { double n, mean, m2; };
-
-__device__ __forceinline__ void push(Moments& s, double x) {
-    s.n += 1.0;
-    const double d = x - s.mean;
-    s.mean += d / s.n;
-    s.m2 += d * (x - s.mean);
-}
 
 __device__ __forceinline__ Moments merge(const Moments& a, const Moments& b) {
     if (a.n == 0.0) return b;
@@ -63,15 +56,39 @@ __device__ void block_merge(Moments (&m)[V]) {
     }
 }
 
+// Per-thread running sums about a shift k (the thread's first value): n, sum (x - k) and
+// sum (x - k)^2, turned into a (count, mean, M2) triple once at the end of the thread's range.
+// No division per sample (an FP64 division is a dozen FP64 operations, on a part whose FP64 rate
+// is a small fraction of its FP32 rate); the shift keeps the second sum free of the cancellation
+// of raw moments.
+struct ShiftSums { double n, k, s1, s2; };
+
+__device__ __forceinline__ void add(ShiftSums& a, double x) {
+    if (a.n == 0.0) a.k = x;
+    const double d = x - a.k;
+    a.n += 1.0;
+    a.s1 += d;
+    a.s2 = fma(d, d, a.s2);
+}
+
+__device__ __forceinline__ Moments moments_of(const ShiftSums& a) {
+    if (a.n == 0.0) return Moments{0, 0, 0};
+    const double md = a.s1 / a.n;
+    return Moments{a.n, a.k + md, fmax(0.0, a.s2 - a.s1 * md)};
+}
+
+// the reference's per-sample terms (stats.py:42-48), one division per sample: h1 = 1 / (2 db),
+// h2 = 1 / db^2
 __device__ __forceinline__ void terms(const double* rho, const double* g, const double* gp,
-                                      const double* gm, int64_t i, double db, double& r,
+                                      const double* gm, int64_t i, double h1, double h2, double& r,
                                       double& s1, double& s2) {
     const double rh = rho[i], gg = g[i];
-    r = gg / rh;                                             // stats.py:42
+    const double inv = 1.0 / rh;
+    r = gg * inv;                                            // g / rho
     if (gp) {
         const double p = gp[i], m = gm[i];
-        s1 = (p - m) / rh / (2.0 * db);                      // stats.py:44-45
-        s2 = (p - 2.0 * gg + m) / rh / (db * db);            // stats.py:47-48
+        s1 = (p - m) * inv * h1;                             // (g+ - g-) / rho / (2 db)
+        s2 = (p - 2.0 * gg + m) * inv * h2;                  // (g+ - 2g + g-) / rho / db^2
     } else {
         s1 = 0.0;
         s2 = 0.0;
@@ -80,15 +97,17 @@ __device__ __forceinline__ void terms(const double* rho, const double* g, const 
 
 __global__ void terms_partial(const double* rho, const double* g, const double* gp, const double* gm,
                               int64_t X, double db, double* scratch) {
-    Moments m[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const double h1 = 0.5 / db, h2 = 1.0 / (db * db);
+    ShiftSums acc[3] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < X;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double r, s1, s2;
-        terms(rho, g, gp, gm, i, db, r, s1, s2);
-        push(m[0], r);
-        push(m[1], s1);
-        push(m[2], s2);
+        terms(rho, g, gp, gm, i, h1, h2, r, s1, s2);
+        add(acc[0], r);
+        add(acc[1], s1);
+        add(acc[2], s2);
     }
+    Moments m[3] = {moments_of(acc[0]), moments_of(acc[1]), moments_of(acc[2])};
     block_merge<3>(m);
     if (threadIdx.x == 0)
         for (int v = 0; v < 3; ++v) {
@@ -102,19 +121,21 @@ __global__ void jackknife_partial(const double* rho, const double* g, const doub
                                   const double* totals, double* scratch) {
     const double Sr = totals[0], S1 = totals[1], S2 = totals[2];
     const double E0 = -S1 / Sr;
-    Moments m[2] = {{0, 0, 0}, {0, 0, 0}};
+    const double h1 = 0.5 / db, h2 = 1.0 / (db * db), inv_kT2 = 1.0 / kT2;
+    ShiftSums acc[2] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < X;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         double r, s1, s2;
-        terms(rho, g, gp, gm, i, db, r, s1, s2);
+        terms(rho, g, gp, gm, i, h1, h2, r, s1, s2);
         // f_E,i - E0 and f_C,i - C0 written without the cancellation of the direct differences:
         //   (S - x_i)/(S_r - r_i) - S/S_r = -(S_r x_i - S r_i) / (S_r (S_r - r_i))
-        const double den = Sr * (Sr - r);
-        const double dE = (Sr * s1 - S1 * r) / den;
-        const double dC = (-(Sr * s2 - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2;
-        push(m[0], dE);
-        push(m[1], dC);
+        const double inv_den = 1.0 / (Sr * (Sr - r));
+        const double dE = (Sr * s1 - S1 * r) * inv_den;
+        const double dC = (-(Sr * s2 - S2 * r) * inv_den - dE * (2.0 * E0 + dE)) * inv_kT2;
+        add(acc[0], dE);
+        add(acc[1], dC);
     }
+    Moments m[2] = {moments_of(acc[0]), moments_of(acc[1])};
     block_merge<2>(m);
     if (threadIdx.x == 0)
         for (int v = 0; v < 2; ++v) {
@@ -155,14 +176,16 @@ __global__ void terms_partial_seg(const double* rho, const double* g, const doub
     const int64_t s0 = seg[m], s1 = seg[m + 1];
     const int64_t len = s1 - s0, chunk = (len + kSegChunks - 1) / kSegChunks;
     const int64_t c0 = s0 + c * chunk, c1 = min(s1, c0 + chunk);
-    Moments mo[3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    const double db = dbeta[m], h1 = 0.5 / db, h2 = 1.0 / (db * db);
+    ShiftSums acc[3] = {{0, 0, 0, 0}, {0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
         double r, a, b;
-        terms(rho, g, gp, gm, i, dbeta[m], r, a, b);
-        push(mo[0], r);
-        push(mo[1], a);
-        push(mo[2], b);
+        terms(rho, g, gp, gm, i, h1, h2, r, a, b);
+        add(acc[0], r);
+        add(acc[1], a);
+        add(acc[2], b);
     }
+    Moments mo[3] = {moments_of(acc[0]), moments_of(acc[1]), moments_of(acc[2])};
     block_merge<3>(mo);
     if (threadIdx.x == 0)
         for (int v = 0; v < 3; ++v) {
@@ -181,16 +204,18 @@ __global__ void jackknife_partial_seg(const double* rho, const double* g, const 
     const double* mm = moments + m * 7;
     const double Sr = mm[0] * mm[1], S1 = mm[0] * mm[3], S2 = mm[0] * mm[5];
     const double E0 = -S1 / Sr;
-    Moments mo[2] = {{0, 0, 0}, {0, 0, 0}};
+    const double db = dbeta[m], h1 = 0.5 / db, h2 = 1.0 / (db * db), inv_kT2 = 1.0 / kT2[m];
+    ShiftSums acc[2] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
     for (int64_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) {
         double r, a, b;
-        terms(rho, g, gp, gm, i, dbeta[m], r, a, b);
-        const double den = Sr * (Sr - r);
-        const double dE = (Sr * a - S1 * r) / den;
-        const double dC = (-(Sr * b - S2 * r) / den - dE * (2.0 * E0 + dE)) / kT2[m];
-        push(mo[0], dE);
-        push(mo[1], dC);
+        terms(rho, g, gp, gm, i, h1, h2, r, a, b);
+        const double inv_den = 1.0 / (Sr * (Sr - r));
+        const double dE = (Sr * a - S1 * r) * inv_den;
+        const double dC = (-(Sr * b - S2 * r) * inv_den - dE * (2.0 * E0 + dE)) * inv_kT2;
+        add(acc[0], dE);
+        add(acc[1], dC);
     }
+    Moments mo[2] = {moments_of(acc[0]), moments_of(acc[1])};
     block_merge<2>(mo);
     if (threadIdx.x == 0)
         for (int v = 0; v < 2; ++v) {
