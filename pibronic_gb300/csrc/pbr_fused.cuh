@@ -801,13 +801,15 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 
         // ============================ phase D: outputs ==========================================
         if (active && g == 0) {
+            // traces summed in T: each diagonal entry already carries T's rounding, which a wider
+            // sum would not remove; one conversion per coefficient
             double coef[K + 1];
 #pragma unroll
             for (int k = 0; k <= K; ++k) {
-                double tr = 0.0;
+                T tr = T(0);
 #pragma unroll
-                for (int r = 0; r < A; ++r) tr += static_cast<double>(nser[k][r][r]);
-                coef[k] = scale_pow2(tr, nexp);
+                for (int r = 0; r < A; ++r) tr += nser[k][r][r];
+                coef[k] = scale_pow2(static_cast<double>(tr), nexp);
             }
             double rho = 0.0;
 #pragma unroll

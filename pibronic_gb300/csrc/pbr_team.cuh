@@ -540,13 +540,14 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
             double coef[K + 1];
 #pragma unroll
             for (int k = 0; k <= K; ++k) {
-                double d = 0.0;
+                // the trace summed in T across the team (the entries carry T's rounding already)
+                T d = T(0);
 #pragma unroll
-                for (int c = 0; c < A; ++c) d = (c == r) ? static_cast<double>(nrow[k][c]) : d;
-                if (r >= A) d = 0.0;
+                for (int c = 0; c < A; ++c) d = (c == r) ? nrow[k][c] : d;
+                if (r >= A) d = T(0);
 #pragma unroll
                 for (int o = TA / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, TA);
-                coef[k] = scale_pow2(d, nexp);
+                coef[k] = scale_pow2(static_cast<double>(d), nexp);
             }
             double rho = (r < A && r < nfill) ? exp_out<T>(lr_d) : 0.0;
 #pragma unroll

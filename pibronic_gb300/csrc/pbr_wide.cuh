@@ -470,11 +470,11 @@ __device__ void wide_sample(const WideArgs& args, float* sm, const WidePlan& pla
         double coef[K + 1];
 #pragma unroll
         for (int k = 0; k <= K; ++k) {
-            const double d0 = (r < A) ? static_cast<double>(own[(k * AP + r) * AP + r]) : 0.0;
-            double d = d0;
+            // the trace summed in FP32 across the team (the entries carry FP32 rounding already)
+            float d = (r < A) ? own[(k * AP + r) * AP + r] : 0.f;
 #pragma unroll
             for (int o = kWideTeam / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, kWideTeam);
-            coef[k] = scale_pow2(d, nexp);
+            coef[k] = scale_pow2(static_cast<double>(d), nexp);
         }
         double rho = (r < nfill) ? exp_out<float>(lr_d) : 0.0;
 #pragma unroll
