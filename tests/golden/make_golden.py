@@ -184,11 +184,11 @@ def run_ml_case(engine, fs, case):
 
 
 CASES = {
-    # BASELINE config 1 shapes: A=2, N=2, P=12, T=300 K, quadratic terms, dbeta = 1e-4 beta
+    # the smallest benchmark shapes: A=2, N=2, P=12, T=300 K, quadratic terms, dbeta = 1e-4 beta
     "cfg1": dict(A=2, N=2, P=12, T=300.0, X=400, B=100, model_seed=11, rng_seed=1234),
-    # config 2 shapes at a small sample count: A=4, N=12, P=64
+    # the main benchmark shapes at a small sample count: A=4, N=12, P=64
     "cfg2": dict(A=4, N=12, P=64, T=300.0, X=60, B=20, model_seed=22, rng_seed=4321),
-    # config 2 at the low temperature of its sweep
+    # the same shapes at the low temperature of their sweep
     "cfg2_cold": dict(A=4, N=12, P=64, T=100.0, X=40, B=20, model_seed=23, rng_seed=99),
     # odd bead count, three surfaces, strong off-diagonal couplings
     "odd": dict(A=3, N=5, P=7, T=250.0, X=50, B=25, model_seed=5, rng_seed=77, sd_offdiag=0.1),
