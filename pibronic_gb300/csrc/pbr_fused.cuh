@@ -281,11 +281,32 @@ template <> struct LogSum<float> {
         s = t;
     }
     __device__ __forceinline__ double value() const { return static_cast<double>(s) - static_cast<double>(c); }
+    // adds another compensated sum: the leading parts by an error-free two-sum, whose rounding
+    // error goes into the compensation (the chunk combine stays in FP32)
+    __device__ __forceinline__ void merge(const LogSum& o) {
+        const float t = s + o.s;
+        const float bp = t - s;
+        const float e = (s - (t - bp)) + (o.s - bp);
+        c = (c + o.c) - e;
+        s = t;
+    }
+    __device__ __forceinline__ LogSum shfl_down(int st, int width) const {
+        LogSum r;
+        r.s = __shfl_down_sync(0xffffffffu, s, st, width);
+        r.c = __shfl_down_sync(0xffffffffu, c, st, width);
+        return r;
+    }
 };
 template <> struct LogSum<double> {
     double s = 0.0;
     __device__ __forceinline__ void add(double x) { s += x; }
     __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ void merge(const LogSum& o) { s += o.s; }
+    __device__ __forceinline__ LogSum shfl_down(int st, int width) const {
+        LogSum r;
+        r.s = __shfl_down_sync(0xffffffffu, s, st, width);
+        return r;
+    }
 };
 
 // Source surface of global sample sg ~ Categorical(state weights) (pimc.py:386-389).
@@ -756,10 +777,6 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
         }
 
         // ============================ phase C: combine the chunks ===============================
-        double lr_d[A];
-#pragma unroll
-        for (int a = 0; a < A; ++a) lr_d[a] = lrho[a].value();
-        double ls_d = lsum.value();
         for (int st = 1; st < G; st <<= 1) {
             T oth[K + 1][A][A];
 #pragma unroll
@@ -793,11 +810,16 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                 nexp += renormalise<T, K, A>(nser);
             }
         }
+        // the chunks' log sums, compensated (FP32 pairs in the FP32 build), summed down to g = 0
         for (int st = G >> 1; st >= 1; st >>= 1) {
 #pragma unroll
-            for (int a = 0; a < A; ++a) lr_d[a] += __shfl_down_sync(0xffffffffu, lr_d[a], st, G);
-            ls_d += __shfl_down_sync(0xffffffffu, ls_d, st, G);
+            for (int a = 0; a < A; ++a) lrho[a].merge(lrho[a].shfl_down(st, G));
+            lsum.merge(lsum.shfl_down(st, G));
         }
+        double lr_d[A];
+#pragma unroll
+        for (int a = 0; a < A; ++a) lr_d[a] = lrho[a].value();
+        const double ls_d = lsum.value();
 
         // ============================ phase D: outputs ==========================================
         if (active && g == 0) {
