@@ -69,7 +69,7 @@ struct TeamPlan {
         int nb = S * P * rl;
         nb = nb > comb ? nb : comb;
         beads = take(nb);
-        lsums = take((S * G * (A + 2) * 8 + esz - 1) / esz);      // doubles + exponent slot
+        lsums = take((S * G * (A + 2) * 8 + esz - 1) / esz);      // 8-byte log sums + exponent slot
         total_bytes = o * esz;
     }
 };
@@ -140,7 +140,8 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     T* s_q = sm + plan.q;
     T* s_ql = kLo ? sm + plan.qlo : nullptr;
     T* s_beads = sm + plan.beads;
-    double* s_lsum = reinterpret_cast<double*>(sm + plan.lsums);
+    // per combine slot: the team's compensated log sums (rho terms, ln S12), 8 bytes each
+    LogSum<T>* s_lsum = reinterpret_cast<LogSum<T>*>(sm + plan.lsums);
     const int tid = threadIdx.x;
 
 
@@ -467,17 +468,14 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
         T* comb = s_beads;
         int* cexp = reinterpret_cast<int*>(s_lsum + S * G * (A + 1));
         const int slot = ts * G + tc;
-        double lr_d = 0.0, ls_d = 0.0;
         if (tact) {
-            lr_d = lr.value();
-            ls_d = ls.value();
             if (r < A)
 #pragma unroll
                 for (int k = 0; k <= K; ++k)
 #pragma unroll
                     for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
-            if (r < A) s_lsum[slot * (A + 1) + r] = lr_d;
-            if (r == 0) { s_lsum[slot * (A + 1) + A] = ls_d; cexp[slot] = nexp; }
+            if (r < A) s_lsum[slot * (A + 1) + r] = lr;
+            if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
         }
         __syncthreads();
         for (int st = 1; st < G; st <<= 1) {
@@ -502,9 +500,9 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     for (int k = 0; k <= K; ++k)
 #pragma unroll
                         for (int c = 0; c < A; ++c) nrow[k][c] = z[k][c];
-                    lr_d += s_lsum[ps * (A + 1) + r];
+                    lr.merge(s_lsum[ps * (A + 1) + r]);
                 }
-                if (r == 0) ls_d += s_lsum[ps * (A + 1) + A];
+                if (r == 0) ls.merge(s_lsum[ps * (A + 1) + A]);
                 nexp += cexp[ps];
                 T mx = T(0);
                 if (r < A) {
@@ -529,8 +527,8 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     for (int k = 0; k <= K; ++k)
 #pragma unroll
                         for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
-                if (r < A) s_lsum[slot * (A + 1) + r] = lr_d;
-                if (r == 0) { s_lsum[slot * (A + 1) + A] = ls_d; cexp[slot] = nexp; }
+                if (r < A) s_lsum[slot * (A + 1) + r] = lr;
+                if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
             }
             __syncthreads();
         }
@@ -549,6 +547,7 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                 for (int o = TA / 2; o >= 1; o >>= 1) d += __shfl_xor_sync(tmask, d, o, TA);
                 coef[k] = scale_pow2(static_cast<double>(d), nexp);
             }
+            const double lr_d = lr.value(), ls_d = ls.value();
             double rho = (r < A && r < nfill) ? exp_out<T>(lr_d) : 0.0;
 #pragma unroll
             for (int o = TA / 2; o >= 1; o >>= 1) rho += __shfl_xor_sync(tmask, rho, o, TA);
