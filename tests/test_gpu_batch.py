@@ -75,3 +75,33 @@ def test_batch_graph_replay_matches_direct_run():
     for k in direct:
         assert torch.equal(mb.out[k], direct[k])
     assert torch.equal(mb.moments, mom)
+
+
+def test_batch_dispatch_forms_match_single_model_runs():
+    """One batch holding every dispatch path: register-chunk launches per model (up to 4
+    surfaces), the two-block row-team build (5-6 surfaces whose tiles fit twice per SM), the
+    one-block build (a 126 KB tile) and 8 surfaces -- each model against its own single-model run
+    in the library's automatic form and in the row-team form."""
+    from pibronic_gb300 import constants, synthetic
+    from pibronic_gb300.batch import ModelBatch
+    from pibronic_gb300.plan import DevicePlan, PreparedModels
+    from pibronic_gb300.pimc import evaluate_device
+    shapes = [(3, 6, 32), (4, 12, 64), (5, 16, 32), (6, 20, 128), (8, 8, 32), (6, 10, 32)]
+    preps = []
+    for i, (A, N, P) in enumerate(shapes):
+        m = synthetic.make_coupled_model(A, N, 2000 + i, sd_quadratic=0.0005)
+        beta = constants.beta(250.0 + 20 * i)
+        preps.append(PreparedModels(m, synthetic.diagonal_of(m), P, beta=beta, delta_beta=1e-4 * beta))
+    X = [700 + 13 * i for i in range(len(shapes))]
+    seeds = [31 + i for i in range(len(shapes))]
+    mb = ModelBatch(preps, X, seeds)
+    assert mb.groups >= 5
+    mb.run()
+    torch.cuda.synchronize()
+    assert int(mb.status.item()) == 0
+    for i, prep in enumerate(preps):
+        sl = slice(int(mb.seg[i]), int(mb.seg[i + 1]))
+        for variant in (0, 2):
+            single = evaluate_device(DevicePlan(prep, precision=32, variant=variant), X[i], seed=seeds[i], offset=0)
+            for k in ("s_rho", "s_g", "s_gp", "s_gm"):
+                assert torch.allclose(mb.out[k][sl], single[k], rtol=2e-4, atol=0), (shapes[i], variant, k)
