@@ -173,27 +173,34 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                 back_substitute<T>(m, j, dsh, s_q + s * args.qstride + j * rs);
             }
             __syncthreads();
-            if (args.out.q_out || args.out.src_out) {
-                for (int i = tid; i < nvalid * NP; i += NT) {
-                    const int s = i / NP, ii = i - s * NP, j = ii / P, p = ii - j * P;
-                    if (args.out.q_out)
-                        args.out.q_out[(base + s) * static_cast<int64_t>(NP) + ii] =
-                            static_cast<float>(s_q[s * args.qstride + qidx(j, p, rs)]);
+            if (args.out.q_out) {
+                // a warp per (sample, mode) row, lanes over the beads (no per-element division)
+                for (int row = tid >> 5; row < nvalid * N; row += NT >> 5) {
+                    const int s = row / N, j = row - s * N;
+                    float* dst = args.out.q_out + ((base + s) * N + j) * static_cast<int64_t>(P);
+                    const T* src = s_q + s * args.qstride + j * rs;
+                    for (int p = tid & 31; p < P; p += 32) dst[p] = static_cast<float>(src[p + (p >> 5)]);
                 }
-                if (args.out.src_out)
-                    for (int s = tid; s < nvalid; s += NT) args.out.src_out[base + s] = s_src[s];
             }
+            if (args.out.src_out)
+                for (int s = tid; s < nvalid; s += NT) args.out.src_out[base + s] = s_src[s];
         } else {
-            for (int i = tid; i < nvalid * NP; i += NT) {
-                const int s = i / NP, ii = i - s * NP, j = ii / P, p = ii - j * P;
-                const int dst = s * args.qstride + qidx(j, p, rs);
-                if (QM == kQ64) {
-                    const double v = static_cast<const double*>(args.q_in)[(base + s) * static_cast<int64_t>(NP) + ii];
-                    const T hi = T(v);
-                    s_q[dst] = hi;
-                    if (kLo) s_ql[dst] = T(v - static_cast<double>(hi));
-                } else {
-                    s_q[dst] = T(static_cast<const float*>(args.q_in)[(base + s) * static_cast<int64_t>(NP) + ii]);
+            // the caller's q: a warp per (sample, mode) row, lanes over the beads
+            for (int row = tid >> 5; row < nvalid * N; row += NT >> 5) {
+                const int s = row / N, j = row - s * N;
+                const int64_t src0 = ((base + s) * N + j) * static_cast<int64_t>(P);
+                T* dq = s_q + s * args.qstride + j * rs;
+                T* dl = kLo ? s_ql + s * args.qstride + j * rs : nullptr;
+                for (int p = tid & 31; p < P; p += 32) {
+                    const int d = p + (p >> 5);                      // qidx(j, p, rs) - j * rs
+                    if (QM == kQ64) {
+                        const double v = static_cast<const double*>(args.q_in)[src0 + p];
+                        const T hi = T(v);
+                        dq[d] = hi;
+                        if (kLo) dl[d] = T(v - static_cast<double>(hi));
+                    } else {
+                        dq[d] = T(static_cast<const float*>(args.q_in)[src0 + p]);
+                    }
                 }
             }
             __syncthreads();
