@@ -880,9 +880,10 @@ __global__ void __launch_bounds__(kThreads) sample_q_kernel(const FusedArgs args
             if (args.out.src_out && g == 0) args.out.src_out[sidx] = src;
             const int NP = N * P;
             float* qo = args.out.q_out + sidx * static_cast<int64_t>(NP);
+            int j = g / P, p = g - j * P;                     // element i = j P + p, stepped by G
             for (int i = g; i < NP; i += G) {
-                const int j = i / P, p = i - j * P;
                 qo[i] = static_cast<float>(qs[qidx(j, p, rs)]);
+                for (p += G; p >= P; p -= P) ++j;
             }
         }
         __syncwarp();
