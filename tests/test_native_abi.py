@@ -51,3 +51,59 @@ def test_calls_with_a_wrong_argument_count_are_rejected():
         lib.pbr_version(0)
     with pytest.raises(TypeError):
         lib.pbr_reduce_blocks()
+
+
+def _fake_models(shapes, variant=0):
+    """pbr_model / pbr_outputs arrays for the host-only packer: sizes set, table and output
+    pointers non-null but never dereferenced (no device memory on this machine)."""
+    from pibronic_gb300 import _native
+    M = len(shapes)
+    models, outs = (_native.PbrModel * M)(), (_native.PbrOutputs * M)()
+    fake = 0x1000
+    for i, (A, N, P) in enumerate(shapes):
+        m = models[i]
+        m.A = m.A_rho = m.n_fill_rho = A
+        m.N, m.P, m.K, m.precision, m.variant = N, P, 4, 32, variant
+        m.tau, m.delta_beta = 0.01, 1e-3
+        for f in ("vib_cs", "vib_th", "vib_c", "vib_d", "vib_e", "vib_l", "vib_qq", "rho_cs", "rho_th",
+                  "rho_c", "rho_d", "ring_chol", "src_cdf"):
+            setattr(m, f, fake)
+        for f in ("s_rho", "s_g", "s_gp", "s_gm"):
+            setattr(outs[i], f, fake)
+    return models, outs
+
+
+def _pack(lib, shapes, variant=0, budget=0):
+    M = len(shapes)
+    models, outs = _fake_models(shapes, variant)
+    seeds = (ctypes.c_uint64 * M)(*range(1, M + 1))
+    offs = (ctypes.c_uint64 * M)()
+    X = (ctypes.c_int64 * M)(*([1000] * M))
+    blob = ctypes.create_string_buffer(int(lib.pbr_batch_blob_bytes(M)))
+    rc = lib.pbr_batch_pack(models, seeds, offs, X, outs, M, budget, 0, blob)
+    return rc, blob
+
+
+def test_batch_packing_groups_models_by_kernel_form():
+    """The batch packer is host code: models group by surface count, and at 5-6 surfaces by
+    whether two tiles fit an SM (the two-block row-team build) -- here 2, 3, 4 surfaces (one
+    register-chunk group each), 5 and 6 surfaces at P = 32 (two-block), 6 surfaces at N = 20,
+    P = 128 (a 126 KB tile: one-block), 8 surfaces."""
+    from pibronic_gb300 import build, _native
+    lib = _native.load(build.build())
+    shapes = [(2, 4, 16), (3, 6, 32), (4, 12, 64), (5, 16, 32), (6, 10, 32), (6, 20, 128), (8, 8, 32)]
+    rc, blob = _pack(lib, shapes)
+    assert rc == 0
+    assert lib.pbr_batch_groups(blob) == 7
+    # two models that share a group stay in one group
+    rc, blob = _pack(lib, shapes + [(2, 5, 24), (6, 12, 32)])
+    assert rc == 0 and lib.pbr_batch_groups(blob) == 7
+
+
+def test_batch_packing_rejects_bad_models():
+    from pibronic_gb300 import build, _native
+    lib = _native.load(build.build())
+    rc, _ = _pack(lib, [(4, 12, 2000)])           # more beads than the limit
+    assert rc == _native.PBR_ERR_ARG
+    rc, _ = _pack(lib, [(9, 4, 16)])              # more surfaces than the row-team form holds
+    assert rc != 0
