@@ -17,7 +17,8 @@
 //              chunk product  N(h) <- N(h) M_p diag(O-hat_p(h)), renormalised by a power of two.
 //   phase C  chunk products combined in bead order by a shuffle tree within the segment.
 //   phase D  traces: s_g = Tr N_0, g(beta +- db) = sum_k Tr N_k (+-db)^k, s_rho = sum_a exp(sum_p
-//            (phi^rho_pa - ln S12_p)), all in FP64 with the accumulated power-of-two exponent.
+//            (phi^rho_pa - ln S12_p)); the traces summed in the kernel's type, scaled exactly by
+//            the accumulated power-of-two exponent and combined in FP64.
 #pragma once
 
 #include "pbr_common.cuh"
