@@ -204,6 +204,9 @@ CASES = {
     "a8": dict(A=8, N=5, P=16, T=400.0, X=24, B=12, model_seed=88, rng_seed=808),
     # seven surfaces, odd everything
     "a7": dict(A=7, N=3, P=9, T=150.0, X=21, B=7, model_seed=77, rng_seed=707),
+    # more surfaces than the row-team form holds (the tensor-core and wide forms): 12 and 16
+    "a12": dict(A=12, N=4, P=8, T=300.0, X=12, B=6, model_seed=1212, rng_seed=1213),
+    "a16": dict(A=16, N=3, P=6, T=250.0, X=8, B=4, model_seed=1616, rng_seed=1617),
 }
 
 
