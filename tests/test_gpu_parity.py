@@ -162,3 +162,17 @@ def test_stage_scaling_matches_oracle(runs):
     assert np.allclose(S12.cpu().numpy(), ref["S12"], rtol=1e-10)
     assert np.allclose(y_rho, ref["rho"], rtol=1e-9)
     assert np.allclose(y_g, ref["g"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["a12", "a16", "a8"])
+def test_tensor_core_form_matches_reference(runs, name):
+    """The tensor-core form (V(q) by the tcgen05 GEMM; the wide kernel above 8 surfaces, the
+    row-team kernel on the GEMM's V up to 8) on the reference's recorded q, against the
+    reference's outputs at the FP32 production tolerance."""
+    from pibronic_gb300.plan import DevicePlan
+    c = case_of(runs, name)
+    got = _eval(c, 32, variant=DevicePlan.VARIANT_TC)
+    assert np.allclose(got["s_rho"], c["s_rho"], rtol=2e-4, atol=0)
+    assert np.allclose(got["s_g"], c["s_g"], rtol=2e-4, atol=0)
+    assert np.allclose(got["s_gp"], c["s_gP"], rtol=2e-4, atol=0)
+    assert np.allclose(got["s_gm"], c["s_gM"], rtol=2e-4, atol=0)
