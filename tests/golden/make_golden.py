@@ -104,7 +104,10 @@ def write_models(root, case):
     return vib_text, rho_text
 
 
-def run_case(engine, fs, const, case):
+def run_case(engine, fs, const, case, files=None):
+    """Run block_compute(_pm) of the reference on the case; with `files` (a dict), also keep the
+    result file the run wrote (pimc.py:1383, 1461) and two the reference's BoxResult writes and
+    merges around it (pimc.py:819-835, 948-964, 853-912, 975-1040)."""
     root = tempfile.mkdtemp(prefix="pbr_case_")
     vib_text, rho_text = write_models(root, case)
     FS = fs.FileStructure(root, 0, 0)
@@ -148,8 +151,63 @@ def run_case(engine, fs, const, case):
     if pm:
         out["s_gP"] = result.scaled_gofr_plus.copy()
         out["s_gM"] = result.scaled_gofr_minus.copy()
+    if files is not None:
+        keep_result_files(engine, FS, data, result, pm, files)
     shutil.rmtree(root, ignore_errors=True)
     return out
+
+
+def keep_result_files(engine, FS, data, result, pm, files):
+    """The run's own file (J0), a second job's file written by the reference from doubled arrays
+    (J1), a file of the other result class (J2: its keys are a subset or a superset), and the
+    reference's merge of the three; merge order follows a Python set, so the merged arrays are
+    recorded sorted by s_rho."""
+    cls = engine.BoxResultPM if pm else engine.BoxResult
+    other = engine.BoxResult if pm else engine.BoxResultPM
+    path0 = result.compute_path_to_file()
+    second = cls(data=data)
+    second.path_root, second.id_job = result.path_root, 1
+    second.scaled_rho, second.scaled_g = 2.0 * result.scaled_rho, 2.0 * result.scaled_g
+    if pm:
+        second.scaled_gofr_plus = 2.0 * result.scaled_gofr_plus
+        second.scaled_gofr_minus = 2.0 * result.scaled_gofr_minus
+    second.save_results(data.samples)
+    path1 = second.compute_path_to_file()
+    third = other(data=data)
+    third.path_root, third.id_job = result.path_root, 2
+    third.scaled_rho, third.scaled_g = 3.0 * result.scaled_rho, 3.0 * result.scaled_g
+    if not pm:
+        third.scaled_gofr_plus = 3.0 * result.scaled_rho
+        third.scaled_gofr_minus = 3.0 * result.scaled_g
+    third.save_results(data.samples)
+    path2 = third.compute_path_to_file()
+    for j, path in enumerate((path0, path1, path2)):
+        files[f"name_J{j}"] = np.array(os.path.basename(path))
+        with open(path, "rb") as fh:
+            files[f"bytes_J{j}"] = np.frombuffer(fh.read(), dtype=np.uint8)
+    merged = cls()
+    merged.load_multiple_results([path0, path1, path2])
+    order = np.argsort(merged.scaled_rho, kind="stable")
+    files["merged_samples"] = np.int64(merged.samples)
+    files["merged_s_rho"] = np.asarray(merged.scaled_rho)[order]
+    files["merged_s_g"] = np.asarray(merged.scaled_g)[order]
+    if pm:
+        files["merged_s_gP"] = np.asarray(merged.scaled_gofr_plus)[order]
+        files["merged_s_gM"] = np.asarray(merged.scaled_gofr_minus)[order]
+    files["P"], files["T"] = np.int64(data.beads), np.float64(data.temperature)
+    files["hash_vib"], files["hash_rho"] = np.array(data.hash_vib), np.array(data.hash_rho)
+
+
+def result_files(engine, fs, const):
+    """Result files of a beta +- dbeta run (cfg1 shapes) and of a plain run (the `plain` case)."""
+    out = {}
+    for tag, name in (("pm", "cfg1"), ("plain", "plain")):
+        files = {}
+        run_case(engine, fs, const, dict(CASES[name], X=12, B=6), files=files)
+        for k, v in files.items():
+            out[f"{tag}/{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "reference_result_files.npz"), **out)
+    return sorted(out)
 
 
 def run_ml_case(engine, fs, case):
@@ -248,6 +306,7 @@ def main(ref_root="/root/reference"):
     np.savez_compressed(os.path.join(HERE, "reference_runs.npz"), **runs)
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(CASES, fh, indent=1)
+    print("reference_result_files.npz:", result_files(engine, fs, const))
     shutil.rmtree(tmp, ignore_errors=True)
     print("wrote", os.path.join(HERE, "reference_runs.npz"))
 
