@@ -8,6 +8,7 @@ estimators (pbr_reduce_jackknife).  Only a handful of doubles come back to the h
 """
 from __future__ import annotations
 
+import json
 import math
 
 import numpy as np
@@ -19,7 +20,8 @@ from .constants import boltzman
 
 __all__ = ["calculate_alpha_terms", "add_harmonic_contribution", "estimate_basic_properties",
            "calculate_basic_property_terms", "basic_statistical_analysis", "alpha_statistical_analysis",
-           "basic_jackknife_analysis", "device_estimates", "ess"]
+           "basic_jackknife_analysis", "alpha_jackknife_analysis", "statistical_analysis_of_pimc",
+           "jackknife_analysis_of_pimc", "device_estimates", "ess"]
 
 
 def calculate_basic_property_terms(*args):
@@ -94,20 +96,92 @@ def alpha_statistical_analysis(temperature, pimc_result, analytic_data, delta_be
     return out
 
 
-def basic_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta):
-    """stats.py:271-301 (with the run's delta_beta passed explicitly)."""
-    data = [pimc_result.scaled_rho, pimc_result.scaled_g, pimc_result.scaled_gofr_plus,
-            pimc_result.scaled_gofr_minus]
-    X = pimc_result.samples
-    terms = calculate_basic_property_terms(delta_beta, *data)
-    jk_terms = jk.calculate_jackknife_terms(X, terms)
-    basic = estimate_basic_properties(X, temperature, *terms)
-    jkd = jk.estimate_jackknife(X, temperature, delta_beta, basic, *jk_terms)
+def _with_jackknife(basic, jkd, analytic_data):
     add_harmonic_contribution(basic, analytic_data["E"], analytic_data["Cv"])
     add_harmonic_contribution(jkd, analytic_data["E"], analytic_data["Cv"])
     out = dict(basic)
     out.update({"jk_" + k: v for k, v in jkd.items()})
     return out
+
+
+def basic_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta=constants.delta_beta):
+    """stats.py:271-299: the basic estimates plus their jackknife ("jk_" keys).  The reference
+    always uses the module constant delta_beta; a run made with another step passes its own."""
+    X = pimc_result.samples
+    terms = calculate_basic_property_terms(delta_beta, *_result_arrays(pimc_result))
+    jk_terms = jk.calculate_jackknife_terms(X, terms)
+    basic = estimate_basic_properties(X, temperature, *terms)
+    jkd = jk.estimate_jackknife(X, temperature, delta_beta, basic, *jk_terms)
+    return _with_jackknife(basic, jkd, analytic_data)
+
+
+def alpha_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta=constants.delta_beta):
+    """stats.py:302-333: the alpha estimates plus their jackknife, whose leave-one-out terms weight
+    g(beta +- dbeta) / rho by the closed-form alpha_pm (jackknife.py:14-57)."""
+    X = pimc_result.samples
+    terms = calculate_alpha_terms(delta_beta, *_result_arrays(pimc_result), analytic_data["alpha_plus"],
+                                  analytic_data["alpha_minus"])
+    jk_terms = jk.calculate_alpha_jackknife_terms(X, delta_beta, terms[0], *terms[3:7])
+    alpha = estimate_basic_properties(X, temperature, *terms[:-4])
+    jkd = jk.estimate_jackknife(X, temperature, delta_beta, alpha, *jk_terms)
+    return _with_jackknife(alpha, jkd, analytic_data)
+
+
+# ---------------------------------------------------------------------------------------------
+# file-driven analyses (one *_thermo file per (P, T) found among the data set's result files)
+# ---------------------------------------------------------------------------------------------
+def starmap_wrapper(FS, P, T, statistical_operation):
+    """Merge every job's results at (P, T), read the analytic data at T, run the operation and
+    write its dict with the model hashes to P{P}_T{T:.2f}_X{X}_thermo (stats.py:148-179)."""
+    from . import postprocessing as pp
+    from .pimc import BoxResultPM
+    pimc_results = BoxResultPM()
+    rho_data = {}
+    pp.load_pimc_data(FS, P, T, pimc_results)
+    pp.load_analytic_data(FS, T, rho_data)
+    out = statistical_operation(T, pimc_results, rho_data)
+    if not (hasattr(FS, "hash_vib") and hasattr(FS, "hash_rho")):
+        raise AttributeError(f"FS {FS} doesn't have hash_vib or hash_rho attributes!")
+    out["hash_vib"], out["hash_rho"] = FS.hash_vib, FS.hash_rho
+    assert pimc_results.samples != 0, "pimc_results has 0 samples! reading the data failed?!"
+    path = FS.template_jackknife.format(P=P, T=T, X=int(pimc_results.samples))
+    with open(path, mode="w", encoding="UTF8") as fh:
+        fh.write(json.dumps({k: (float(v) if isinstance(v, (np.floating, float)) else v)
+                             for k, v in out.items()}))
+    return path
+
+
+_OPERATIONS = {("basic", False): basic_statistical_analysis, ("alpha", False): alpha_statistical_analysis,
+               ("basic", True): basic_jackknife_analysis, ("alpha", True): alpha_jackknife_analysis}
+
+
+def _analysis_of_pimc(FS, method, location, jackknife):
+    from . import postprocessing as pp
+    FS.generate_model_hashes()
+    list_pimc = pp.retrive_pimc_file_list(FS)
+    beads = pp.extract_bead_paramater_list(list_pimc)
+    temperatures = pp.extract_temperature_paramater_list(list_pimc)
+    operation = _OPERATIONS.get((method, jackknife))
+    if operation is None:
+        raise Exception(f"Invalid value for parameter method:({method})")
+    if location == "server":
+        raise AssertionError("Need to write this code")
+    if location != "local":
+        raise Exception(f"Invalid value for parameter location:({location})")
+    return [starmap_wrapper(FS, P, T, operation) for P in beads for T in temperatures]
+
+
+def statistical_analysis_of_pimc(FS, method="basic", location="local", samples=None):
+    """Z, E, Cv ("basic" or "alpha" estimator) for every (P, T) of the data set's result files,
+    one *_thermo file each (stats.py:219-265).  The reference runs the (P, T) pairs in a pool of 12
+    processes; here they run in turn (each is a pass over host arrays); returns the written paths.
+    `samples` is accepted and unused, as in the reference."""
+    return _analysis_of_pimc(FS, method, location, jackknife=False)
+
+
+def jackknife_analysis_of_pimc(FS, method="basic", location="local", samples=None):
+    """As statistical_analysis_of_pimc with the jackknife estimates added (stats.py:336-377)."""
+    return _analysis_of_pimc(FS, method, location, jackknife=True)
 
 
 # ---------------------------------------------------------------------------------------------

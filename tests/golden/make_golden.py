@@ -198,6 +198,67 @@ def keep_result_files(engine, FS, data, result, pm, files):
     files["hash_vib"], files["hash_rho"] = np.array(data.hash_vib), np.array(data.hash_rho)
 
 
+ANALYSIS_JOBS = [  # (P, T, J, X, rng_seed, beta +- dbeta) on the full (P, T) grid the reference
+    # analyses (every pair must have a file): two jobs at one pair, a plain run beside another
+    (12, 300.0, 0, 40, 501, True), (12, 300.0, 1, 40, 502, True), (12, 250.0, 0, 20, 503, True),
+    (8, 300.0, 0, 20, 504, True), (8, 250.0, 0, 30, 505, True), (8, 250.0, 1, 30, 506, False)]
+
+
+def analysis_files(engine, st, fs, const):
+    """A data set with result files from several jobs and an analytic-results file, and the
+    *_thermo files the reference's file-driven estimators write from it
+    (stats.py:148-179, 219-265, 336-377) for each method, basic and alpha, with and without the
+    jackknife.  The analytic file is the package's closed form in the reference's layout (the
+    reference takes it from its Julia toolkit); the estimators only read it."""
+    from pibronic_gb300 import analytic
+    from pibronic_gb300 import file_structure as our_fs
+    import contextlib
+    import io
+    root = tempfile.mkdtemp(prefix="pbr_stats_")
+    case = dict(CASES["cfg1"])
+    vib_text, rho_text = write_models(root, case)
+    FS = fs.FileStructure(root, 0, 0)
+    FS.generate_model_hashes()
+    A = json.loads(vib_text)["number of surfaces"]
+    N = json.loads(vib_text)["number of modes"]
+    out = {"vib_json": np.array(vib_text), "rho_json": np.array(rho_text)}
+    with contextlib.redirect_stdout(io.StringIO()):
+        for P, T, J, X, seed, pm in ANALYSIS_JOBS:
+            data = engine.BoxDataPM(const.delta_beta) if pm else engine.BoxData()
+            data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+            data.hash_vib, data.hash_rho = FS.hash_vib, FS.hash_rho
+            data.states, data.modes = A, N
+            data.samples, data.beads, data.temperature = X, P, T
+            data.block_size = X // 2
+            data.blocks = 2
+            np.random.seed(seed)
+            data.preprocess()
+            result = engine.BoxResultPM(data=data) if pm else engine.BoxResult(data=data)
+            result.path_root, result.id_job = FS.path_rho_results, J
+            (engine.block_compute_pm if pm else engine.block_compute)(data, result)
+        ours = our_fs.FileStructure(root, 0, 0)
+        for T in sorted({job[1] for job in ANALYSIS_JOBS}):
+            analytic.analytic_of_sampling_model(ours, const.beta(T))
+        for path in sorted(glob.glob(os.path.join(FS.path_rho_results, "*.npz"))):
+            name = os.path.basename(path)
+            with open(path, "rb") as fh:
+                out[f"result/{name}"] = np.frombuffer(fh.read(), dtype=np.uint8)
+        with open(FS.path_analytic_rho) as fh:
+            out["analytic_json"] = np.array(fh.read())
+        for method in ("basic", "alpha"):
+            for tag, driver in (("stats", st.statistical_analysis_of_pimc),
+                                ("jk", st.jackknife_analysis_of_pimc)):
+                for path in glob.glob(os.path.join(FS.path_rho_results, "*_thermo")):
+                    os.remove(path)
+                driver(FS, method=method)
+                for path in sorted(glob.glob(os.path.join(FS.path_rho_results, "*_thermo"))):
+                    with open(path) as fh:
+                        out[f"thermo/{tag}_{method}/{os.path.basename(path)}"] = np.array(fh.read())
+    np.savez_compressed(os.path.join(HERE, "reference_analysis_files.npz"), **out)
+    shutil.rmtree(root, ignore_errors=True)
+    return sorted(out)
+
+
 def result_files(engine, fs, const):
     """Result files of a beta +- dbeta run (cfg1 shapes) and of a plain run (the `plain` case)."""
     out = {}
@@ -307,6 +368,7 @@ def main(ref_root="/root/reference"):
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(CASES, fh, indent=1)
     print("reference_result_files.npz:", result_files(engine, fs, const))
+    print("reference_analysis_files.npz:", analysis_files(engine, st, fs, const))
     shutil.rmtree(tmp, ignore_errors=True)
     print("wrote", os.path.join(HERE, "reference_runs.npz"))
 
