@@ -9,7 +9,11 @@ explicit_example.npz, and (2) imports the unmodified reference engine from a tem
 (stub modules stand in for matplotlib and `parse`, which the engine never calls), runs
 block_compute_pm, block_compute, the learned-proposal data path and the estimators on seeded
 synthetic models, and records the sampled q and every output into reference_runs.npz, with the
-model files as JSON text.  The fixtures are small; the GPU machine never needs the reference.
+model files as JSON text.  It also records (3) result files the reference wrote and merged
+(reference_result_files.npz), (4) a data set of result files and the *_thermo files the
+reference's file-driven estimators wrote from it (reference_analysis_files.npz), and (5) the job
+scripts' parameter string and what BoxDataPM made of it (reference_job_parameters.npz).  The
+fixtures are small; the GPU machine never needs the reference.
 """
 from __future__ import annotations
 
@@ -259,6 +263,54 @@ def analysis_files(engine, st, fs, const):
     return sorted(out)
 
 
+def job_parameters(engine, fs, const):
+    """The job scripts' sequence up to the block loop (server/compute_canada/pimc.py:20-36): a
+    parameter dict as the job submitter builds it (server/job_boss.py:415-470), serialised by the
+    reference's BoxData.json_serialize, read back by BoxDataPM.from_json_string, preprocess, and
+    the result file name of job "3".  The data set root is recorded as the token @ROOT@."""
+    import contextlib
+    import io
+    root = tempfile.mkdtemp(prefix="pbr_job_")
+    D, R = 2, 1
+    case = dict(CASES["odd"])
+    vib_dir = os.path.join(root, f"data_set_{D}", "parameters")
+    rho_dir = os.path.join(root, f"data_set_{D}", f"rho_{R}", "parameters")
+    tmp_case = tempfile.mkdtemp(prefix="pbr_jobm_")
+    vib_text, rho_text = write_models(tmp_case, case)
+    shutil.rmtree(tmp_case, ignore_errors=True)
+    os.makedirs(vib_dir)
+    os.makedirs(rho_dir)
+    with open(os.path.join(vib_dir, "coupled_model.json"), "w") as fh:
+        fh.write(vib_text)
+    with open(os.path.join(rho_dir, "sampling_model.json"), "w") as fh:
+        fh.write(rho_text)
+    params = {"number_of_samples": 40, "number_of_blocks": 4, "number_of_states": case["A"],
+              "number_of_modes": case["N"], "number_of_beads": case["P"], "temperature": case["T"],
+              "block_size": 10, "delta_beta": 2e-4, "id_data": D, "id_rho": R, "path_root": root,
+              "path_scratch": os.path.join(root, f"data_set_{D}", f"rho_{R}") + "/",
+              "hostname": "node", "partition": None}
+    text = engine.BoxData.json_serialize(params)
+    out = {"json": np.array(text.replace(root, "@ROOT@")), "vib_json": np.array(vib_text),
+           "rho_json": np.array(rho_text)}
+    with contextlib.redirect_stdout(io.StringIO()):
+        data = engine.BoxDataPM.from_json_string(text)
+        fields = {k: getattr(data, k) for k in ("samples", "blocks", "states", "beads", "modes",
+                                                 "temperature", "block_size", "id_data", "id_rho",
+                                                 "beta", "tau", "delta_beta", "hash_vib", "hash_rho")}
+        data.preprocess()
+        fields.update({k + "_pre": getattr(data, k) for k in ("beta", "tau", "beta_plus", "beta_minus",
+                                                              "tau_plus", "tau_minus")})
+        FS = fs.FileStructure.from_boxdata(os.path.normpath(os.path.join(params["path_scratch"], "../..")), data)
+        result = engine.BoxResultPM(data=data)
+        result.path_root, result.id_job = FS.path_rho_results, "3"
+        fields["result_path"] = result.compute_path_to_file().replace(root, "@ROOT@")
+    for k, v in fields.items():
+        out[f"field/{k}"] = np.array(v)
+    np.savez_compressed(os.path.join(HERE, "reference_job_parameters.npz"), **out)
+    shutil.rmtree(root, ignore_errors=True)
+    return sorted(out)
+
+
 def result_files(engine, fs, const):
     """Result files of a beta +- dbeta run (cfg1 shapes) and of a plain run (the `plain` case)."""
     out = {}
@@ -369,6 +421,7 @@ def main(ref_root="/root/reference"):
         json.dump(CASES, fh, indent=1)
     print("reference_result_files.npz:", result_files(engine, fs, const))
     print("reference_analysis_files.npz:", analysis_files(engine, st, fs, const))
+    print("reference_job_parameters.npz:", job_parameters(engine, fs, const))
     shutil.rmtree(tmp, ignore_errors=True)
     print("wrote", os.path.join(HERE, "reference_runs.npz"))
 
