@@ -127,6 +127,11 @@ def alpha_jackknife_analysis(temperature, pimc_result, analytic_data, delta_beta
     return _with_jackknife(alpha, jkd, analytic_data)
 
 
+def apply_parameter_restrictions(args):
+    """A placeholder of the reference that leaves the (P, T) lists unchanged (stats.py:133-145)."""
+    return
+
+
 # ---------------------------------------------------------------------------------------------
 # file-driven analyses (one *_thermo file per (P, T) found among the data set's result files)
 # ---------------------------------------------------------------------------------------------
@@ -159,8 +164,10 @@ def _analysis_of_pimc(FS, method, location, jackknife):
     from . import postprocessing as pp
     FS.generate_model_hashes()
     list_pimc = pp.retrive_pimc_file_list(FS)
-    beads = pp.extract_bead_paramater_list(list_pimc)
-    temperatures = pp.extract_temperature_paramater_list(list_pimc)
+    args = {"pimc_beads": pp.extract_bead_paramater_list(list_pimc),
+            "temperatures": pp.extract_temperature_paramater_list(list_pimc)}
+    apply_parameter_restrictions(args)
+    beads, temperatures = args["pimc_beads"], args["temperatures"]
     operation = _OPERATIONS.get((method, jackknife))
     if operation is None:
         raise Exception(f"Invalid value for parameter method:({method})")

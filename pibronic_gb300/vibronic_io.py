@@ -160,10 +160,15 @@ def extract_dimensions_of_diagonal_model(FS=None, path=None):
     return _dims(_read(path))
 
 
+def _hash(string):
+    """SHA-512 hex digest of a string's UTF-8 bytes (vibronic_model_io.py:293-297)."""
+    return hashlib.sha512(string.encode("UTF-8")).hexdigest()
+
+
 def _hash_file(path):
     assert os.path.isfile(path), f"The path provided is not a valid file! Path:\n{path}"
     with open(path, mode="r", encoding="UTF8") as fh:
-        return hashlib.sha512(fh.read().encode("UTF-8")).hexdigest()
+        return _hash(fh.read())
 
 
 def create_model_hash(FS=None, path=None):
