@@ -12,7 +12,8 @@ synthetic models, and records the sampled q and every output into reference_runs
 model files as JSON text.  It also records (3) result files the reference wrote and merged
 (reference_result_files.npz), (4) a data set of result files and the *_thermo files the
 reference's file-driven estimators wrote from it (reference_analysis_files.npz), and (5) the job
-scripts' parameter string and what BoxDataPM made of it (reference_job_parameters.npz).  The
+scripts' parameter string and what BoxDataPM made of it (reference_job_parameters.npz), and (6) the
+learned-proposal training files (reference_training_files.npz).  The
 fixtures are small; the GPU machine never needs the reference.
 """
 from __future__ import annotations
@@ -323,8 +324,12 @@ def result_files(engine, fs, const):
     return sorted(out)
 
 
-def run_ml_case(engine, fs, case):
-    """block_compute_gR_from_raw_samples + block_compute_rhoR_from_input_samples."""
+ML_CASE = dict(A=2, N=3, P=8, T=300.0, X=30, B=15, model_seed=17, rng_seed=2024, zero_diag_linear=True)
+
+
+def run_ml_case(engine, fs, case, files=None):
+    """block_compute_gR_from_raw_samples + block_compute_rhoR_from_input_samples; with `files`
+    (a dict), also keep the training files the first wrote (pimc.py:1250-1270, 1305-1338)."""
     root = tempfile.mkdtemp(prefix="pbr_ml_")
     vib_text, rho_text = write_models(root, case)
     FS = fs.FileStructure(root, 0, 0)
@@ -349,6 +354,11 @@ def run_ml_case(engine, fs, case):
             R = d["input_R_values"].copy()
         res2 = engine.BoxResult(data=data)
         engine.block_compute_rhoR_from_input_samples(data, res2, R)
+    if files is not None:
+        for path in sorted(glob.glob(os.path.join(FS.path_vib_results, "*_training_data_*.npz"))):
+            with open(path, "rb") as fh:
+                files[os.path.basename(path)] = np.frombuffer(fh.read(), dtype=np.uint8)
+        files["P"], files["T"], files["X"] = np.int64(case["P"]), np.float64(case["T"]), np.int64(case["X"])
     shutil.rmtree(root, ignore_errors=True)
     return {"R": R, "g": g, "rho": res2.scaled_rho.copy(), "vib_json": np.array(vib_text),
             "rho_json": np.array(rho_text)}
@@ -412,10 +422,11 @@ def main(ref_root="/root/reference"):
     for k, v in jkd.items():
         runs[f"stats/jk/{k}"] = np.float64(v)
     # learned-proposal data path
-    ml = run_ml_case(engine, fs, dict(A=2, N=3, P=8, T=300.0, X=30, B=15, model_seed=17, rng_seed=2024,
-                                      zero_diag_linear=True))
+    training = {}
+    ml = run_ml_case(engine, fs, ML_CASE, files=training)
     for k, v in ml.items():
         runs[f"ml/{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "reference_training_files.npz"), **training)
     np.savez_compressed(os.path.join(HERE, "reference_runs.npz"), **runs)
     with open(os.path.join(HERE, "cases.json"), "w") as fh:
         json.dump(CASES, fh, indent=1)

@@ -112,3 +112,31 @@ def test_load_rejects_a_file_of_another_sample_count(ref_files, tmp_path):
     res = pimc.BoxResultPM(X=5)
     with pytest.raises(AssertionError):
         res.load_results(path)
+
+
+def test_training_files_match_the_reference(tmp_path):
+    """save_gR_with_samples (pimc.py:1250-1270) against the training files the reference's
+    block_compute_gR_from_raw_samples wrote: same names, keys, dtypes and values."""
+    with np.load(os.path.join(GOLDEN, "reference_training_files.npz")) as f:
+        ref = {k: f[k] for k in f.files}
+    names = sorted(k for k in ref if k.endswith(".npz"))
+    (tmp_path / "ref").mkdir()
+    loaded = {}
+    for name in names:
+        path = tmp_path / "ref" / name
+        path.write_bytes(ref[name].tobytes())
+        with np.load(path) as d:
+            loaded[name] = {k: d[k] for k in d.files}
+    g_name = next(n for n in names if n.endswith("_g_output.npz"))
+    in_name = next(n for n in names if n.endswith("_input.npz"))
+    data = SimpleNamespace(beads=int(ref["P"]), temperature=float(ref["T"]), samples=int(ref["X"]),
+                           hash_vib="v", hash_rho="r")
+    res = pimc.BoxResult(data=data)
+    res.path_root, res.id_job = str(tmp_path), 0
+    res.scaled_g = loaded[g_name]["g"].copy()
+    pimc.save_gR_with_samples(data, res, loaded[in_name]["input_R_values"])
+    for name in names:
+        with np.load(tmp_path / name) as d:
+            assert sorted(d.files) == sorted(loaded[name]), name
+            for k, v in loaded[name].items():
+                assert d[k].dtype == v.dtype and np.array_equal(d[k], v), (name, k)
