@@ -145,24 +145,40 @@ def workload_config():
 # GPU side
 # ---------------------------------------------------------------------------------------------
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms.  start() returns once the first
+    sample is on file (nvidia-smi takes a moment to come up); mark() at the start of the timed
+    region sets aside the samples taken before it, so the median is of samples under load."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self, index):
-        self.index, self.proc, self.path = index, None, None
+        self.index, self.proc, self.path, self.skip = index, None, None, 0
 
-    def start(self):
+    def _lines(self):
+        with open(self.path) as fh:
+            return [ln for ln in fh.read().split("\n")[:-1] if ln.strip()]
+
+    def start(self, wait_s=5.0):
         try:
             fd, self.path = tempfile.mkstemp(prefix="pbr_clk_", suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        t_end = time.monotonic() + wait_s
+        while time.monotonic() < t_end and self.proc.poll() is None and not self._lines():
+            time.sleep(0.02)
+
+    def mark(self):
+        """Samples on file now were taken before the timed region."""
+        if self.proc is not None:
+            self.skip = len(self._lines())
 
     def stop(self):
         if self.proc is None:
@@ -173,20 +189,24 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
         rows = []
-        for line in open(self.path):
+        for i, line in enumerate(self._lines()):
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 7:
                 try:
-                    rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+                    rows.append((i, float(parts[0]), float(parts[1]), parts[3:7]))
                 except ValueError:
                     pass
         os.unlink(self.path)
-        if not rows:
+        inside = [r for r in rows if r[0] >= self.skip]
+        # a timed region shorter than the period may hold no sample: report the last one before
+        # it, with samples = 0
+        use = inside if inside else rows[-1:]
+        if not use:
             return None
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, f in rows for i, v in enumerate(f) if v.lower() == "active"})
-        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for _, _, _, f in use for i, v in enumerate(f) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in use), "sm_max_mhz": max(r[2] for r in use),
+                "reasons": reasons, "samples": len(inside), "period_ms": self.PERIOD_MS}
 
 
 def fp32_peak(torch, lib, stream):
@@ -295,6 +315,7 @@ def run_ours(args):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     torch.cuda.synchronize()
+    clocks.mark()
     for s in range(args.steps):
         flush.fill_(float(s))                      # L2 flush between timed steps (untimed)
         e0, e1, e2 = ev[s]
@@ -684,7 +705,7 @@ def batched_leg(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--samples", type=int, default=1_000_000, help="samples per step per GPU")
