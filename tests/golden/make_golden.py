@@ -388,6 +388,11 @@ CASES = {
     # more surfaces than the row-team form holds (the tensor-core and wide forms): 12 and 16
     "a12": dict(A=12, N=4, P=8, T=300.0, X=12, B=6, model_seed=1212, rng_seed=1213),
     "a16": dict(A=16, N=3, P=6, T=250.0, X=8, B=4, model_seed=1616, rng_seed=1617),
+    # the smallest ring the reference accepts (3 beads) with a single mode
+    "p3_n1": dict(A=2, N=1, P=3, T=500.0, X=30, B=10, model_seed=31, rng_seed=313),
+    # hot (1000 K, short tau) and cold (50 K, long tau) ends of the temperature range
+    "hot": dict(A=3, N=4, P=16, T=1000.0, X=30, B=15, model_seed=1000, rng_seed=1001),
+    "frozen": dict(A=2, N=3, P=32, T=50.0, X=20, B=10, model_seed=50, rng_seed=51),
 }
 
 

@@ -8,7 +8,7 @@ import pytest
 from conftest import case_of, oracle_box_from_case
 
 
-@pytest.mark.parametrize("name", ["cfg2", "a8", "a12", "odd"])
+@pytest.mark.parametrize("name", ["cfg2", "a8", "a12", "odd", "hot", "frozen"])
 @pytest.mark.parametrize("shift", [1, 5])
 def test_cyclic_bead_relabelling_leaves_outputs_unchanged(runs, name, shift):
     c = case_of(runs, name)

@@ -37,7 +37,8 @@ def test_ring_basis_is_orthonormal_eigenbasis():
 
 
 @pytest.mark.parametrize("name", ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho",
-                                  "single_surface", "testmodel", "cfg4", "a8", "a7"])
+                                  "single_surface", "testmodel", "cfg4", "a8", "a7", "p3_n1",
+                                  "hot", "frozen"])
 def test_kernel_formulation_matches_oracle(runs, name):
     c = case_of(runs, name)
     q = c["q"]
