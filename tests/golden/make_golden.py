@@ -13,7 +13,8 @@ model files as JSON text.  It also records (3) result files the reference wrote 
 (reference_result_files.npz), (4) a data set of result files and the *_thermo files the
 reference's file-driven estimators wrote from it (reference_analysis_files.npz), and (5) the job
 scripts' parameter string and what BoxDataPM made of it (reference_job_parameters.npz), and (6) the
-learned-proposal training files (reference_training_files.npz).  The
+learned-proposal training files (reference_training_files.npz), and packs (7) the sum-over-states
+results the reference's test data sets carry (reference_sos_results.npz).  The
 fixtures are small; the GPU machine never needs the reference.
 """
 from __future__ import annotations
@@ -67,6 +68,25 @@ def explicit_example(ref_root):
         with open(os.path.join(src, name + ".json")) as fh:
             out[name + "_json"] = np.array(fh.read())
     np.savez_compressed(os.path.join(HERE, "explicit_example.npz"), **out)
+    return sorted(out)
+
+
+def sos_results(ref_root):
+    """The reference's test data sets (tests/test_models/data_set_{0,1}): the coupled and sampling
+    model files with the sum-over-states thermodynamics its Julia toolkit wrote beside them
+    (sos_B60.json, sos_B80.json: Z, E, Cv of the coupled, harmonic and sampling models at 300 K,
+    and Z_sampling at beta +- dbeta)."""
+    src = os.path.join(ref_root, "tests", "test_models")
+    out = {}
+    for path in sorted(glob.glob(os.path.join(src, "data_set_*", "**", "sos_B*.json"), recursive=True)):
+        rel = os.path.relpath(path, src)
+        pdir = os.path.dirname(path)
+        model = "sampling_model.json" if "rho_" in rel else "coupled_model.json"
+        with open(path) as fh:
+            out[f"{rel}/sos"] = np.array(fh.read())
+        with open(os.path.join(pdir, model)) as fh:
+            out[f"{rel}/model"] = np.array(fh.read())
+    np.savez_compressed(os.path.join(HERE, "reference_sos_results.npz"), **out)
     return sorted(out)
 
 
@@ -399,6 +419,7 @@ CASES = {
 def main(ref_root="/root/reference"):
     keys = explicit_example(ref_root)
     print("explicit_example.npz:", keys)
+    print("reference_sos_results.npz:", sos_results(ref_root))
     engine, st, jk, fs, const, tmp = import_reference(ref_root)
     runs = {}
     for name, case in CASES.items():
