@@ -182,7 +182,7 @@ def create_diagonal_model_hash(FS=None, path=None):
 
 
 def remove_coupling_from_model(path_source, path_destination):
-    """Diagonal model from the surface diagonal of a coupled one (vibronic_model_io.py:735-747)."""
+    """Diagonal model from the surface diagonal of a coupled one (vibronic_model_io.py:749-761)."""
     model = load_model_from_JSON(path_source)
     for key, value in list(model.items()):
         if isinstance(value, np.ndarray) and value.ndim >= 2:
@@ -191,6 +191,7 @@ def remove_coupling_from_model(path_source, path_destination):
 
 
 def create_harmonic_model(FS):
+    """The coupled model without its off-diagonal couplings (vibronic_model_io.py:764-771)."""
     remove_coupling_from_model(FS.path_vib_model, FS.path_har_model)
     return FS.path_har_model
 

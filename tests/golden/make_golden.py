@@ -14,7 +14,8 @@ model files as JSON text.  It also records (3) result files the reference wrote 
 reference's file-driven estimators wrote from it (reference_analysis_files.npz), and (5) the job
 scripts' parameter string and what BoxDataPM made of it (reference_job_parameters.npz), and (6) the
 learned-proposal training files (reference_training_files.npz), and packs (7) the sum-over-states
-results the reference's test data sets carry (reference_sos_results.npz).  The
+results the reference's test data sets carry (reference_sos_results.npz), and (8) the diagonal
+models the reference derives from coupled ones (reference_derived_models.npz).  The
 fixtures are small; the GPU machine never needs the reference.
 """
 from __future__ import annotations
@@ -87,6 +88,37 @@ def sos_results(ref_root):
         with open(os.path.join(pdir, model)) as fh:
             out[f"{rel}/model"] = np.array(fh.read())
     np.savez_compressed(os.path.join(HERE, "reference_sos_results.npz"), **out)
+    return sorted(out)
+
+
+def derived_models(ref_root):
+    """The reference's remove_coupling_from_model (vibronic_model_io.py:749-761) on its test data
+    sets' coupled models and on two synthetic ones: input and output model files as text."""
+    import pibronic.vibronic.vibronic_model_io as vio
+    src = os.path.join(ref_root, "tests", "test_models")
+    texts = {}
+    for path in sorted(glob.glob(os.path.join(src, "data_set_*", "parameters", "coupled_model.json"))):
+        with open(path) as fh:
+            texts[os.path.relpath(path, src)] = fh.read()
+    tmp = tempfile.mkdtemp(prefix="pbr_derived_")
+    for name in ("odd", "cfg4"):
+        case = CASES[name]
+        model = synthetic.make_coupled_model(case["A"], case["N"], case["model_seed"],
+                                             sd_offdiag=case.get("sd_offdiag", 0.05))
+        path = os.path.join(tmp, name + ".json")
+        vibronic_io.save_model_to_JSON(path, model)
+        with open(path) as fh:
+            texts[f"synthetic_{name}"] = fh.read()
+    out = {}
+    for i, (name, text) in enumerate(sorted(texts.items())):
+        src_path, dst_path = os.path.join(tmp, f"in_{i}.json"), os.path.join(tmp, f"out_{i}.json")
+        with open(src_path, "w") as fh:
+            fh.write(text)
+        vio.remove_coupling_from_model(src_path, dst_path)
+        with open(dst_path) as fh:
+            out[f"{name}/coupled"], out[f"{name}/diagonal"] = np.array(text), np.array(fh.read())
+    shutil.rmtree(tmp, ignore_errors=True)
+    np.savez_compressed(os.path.join(HERE, "reference_derived_models.npz"), **out)
     return sorted(out)
 
 
@@ -459,6 +491,7 @@ def main(ref_root="/root/reference"):
     print("reference_result_files.npz:", result_files(engine, fs, const))
     print("reference_analysis_files.npz:", analysis_files(engine, st, fs, const))
     print("reference_job_parameters.npz:", job_parameters(engine, fs, const))
+    print("reference_derived_models.npz:", derived_models(ref_root))
     shutil.rmtree(tmp, ignore_errors=True)
     print("wrote", os.path.join(HERE, "reference_runs.npz"))
 
