@@ -21,7 +21,7 @@ from .constants import boltzman
 __all__ = ["calculate_alpha_terms", "add_harmonic_contribution", "estimate_basic_properties",
            "calculate_basic_property_terms", "basic_statistical_analysis", "alpha_statistical_analysis",
            "basic_jackknife_analysis", "alpha_jackknife_analysis", "statistical_analysis_of_pimc",
-           "jackknife_analysis_of_pimc", "device_estimates", "ess"]
+           "jackknife_analysis_of_pimc", "device_estimates", "device_alpha_estimates", "ess"]
 
 
 def calculate_basic_property_terms(*args):
@@ -255,6 +255,16 @@ def device_estimates(rho, g, gp, gm, temperature, delta_beta):
     red = DeviceReducer(rho.shape[0])
     red.launch(rho, g, gp, gm, delta_beta, temperature)
     return red.read(temperature)
+
+
+def device_alpha_estimates(rho, g, gp, gm, temperature, delta_beta, alpha_plus, alpha_minus):
+    """The alpha estimator and its jackknife (stats.py:58-81, 302-333; jackknife.py:14-57) from
+    CUDA tensors.  Its terms are the basic ones with g(beta +- dbeta) scaled by the constants
+    alpha_pm: (alpha+ g+ - alpha- g-) / (2 db rho) and (alpha+ g+ - 2 g + alpha- g-) / (db^2 rho),
+    and a leave-one-out mean of such a linear combination is the combination of the leave-one-out
+    means.  So the basic reduction kernels run on (rho, g, alpha+ g+, alpha- g-)."""
+    return device_estimates(rho, g, gp * float(alpha_plus), gm * float(alpha_minus), temperature,
+                            delta_beta)
 
 
 def ess(weights):

@@ -176,3 +176,28 @@ def test_statistical_analysis_of_pimc_argument_errors(monkeypatch, temp_FS, rng)
         st.statistical_analysis_of_pimc(temp_FS, location=12)
     assert str(e_info.value) == "Invalid value for parameter location:(12)"
     assert not os.listdir(temp_FS.path_rho_results)
+
+
+def test_alpha_estimators_are_the_basic_ones_on_scaled_g_plus_minus(rng):
+    """The identity device_alpha_estimates relies on: the alpha estimates and their jackknife
+    equal the basic ones with g(beta +- dbeta) multiplied by alpha_pm (host arrays, reference
+    formulas on both sides)."""
+    X, T, db = 500, 275.0, 2e-4
+    r = np.random.default_rng(9)
+    res = BoxResultPM(X=X)
+    res.scaled_rho = r.uniform(0.5, 1.5, X)
+    res.scaled_g = res.scaled_rho * r.uniform(0.8, 1.2, X)
+    res.scaled_gofr_plus = res.scaled_g * (1 - 0.3 * db * r.uniform(0.5, 1.5, X))
+    res.scaled_gofr_minus = res.scaled_g * (1 + 0.3 * db * r.uniform(0.5, 1.5, X))
+    analytic_data = {"E": 0.25, "Cv": 1e-4, "alpha_plus": 1.00011, "alpha_minus": 0.99987}
+    alpha = st.alpha_jackknife_analysis(T, res, analytic_data, db)
+    scaled = BoxResultPM(X=X)
+    scaled.scaled_rho, scaled.scaled_g = res.scaled_rho, res.scaled_g
+    scaled.scaled_gofr_plus = res.scaled_gofr_plus * analytic_data["alpha_plus"]
+    scaled.scaled_gofr_minus = res.scaled_gofr_minus * analytic_data["alpha_minus"]
+    basic = st.basic_jackknife_analysis(T, scaled, analytic_data, db)
+    assert list(alpha) == list(basic)
+    # the two sides round differently (alpha+ mean(r+) against mean(alpha+ r+)); E cancels ~1/db
+    # and its jackknife ~X on top, so FP64 agreement is ~1e-8 relative, not 1e-16
+    for k in alpha:
+        assert np.isclose(alpha[k], basic[k], rtol=1e-7, atol=1e-15), (k, alpha[k], basic[k])
