@@ -76,3 +76,12 @@ def test_too_few_beads_are_rejected(ref, tmp_path):
     data.beads = 2
     with pytest.raises(AssertionError):
         data.preprocess()
+
+
+def test_minimal_module_name_exports_the_engine():
+    """examples/basic_ml_testing.py:17 of the reference imports the engine as pimc.minimal."""
+    from pibronic_gb300 import minimal
+    for name in ("BoxData", "BoxDataPM", "BoxResult", "BoxResultPM", "block_compute", "block_compute_pm",
+                 "block_compute_gR_from_raw_samples", "block_compute_rhoR_from_input_samples",
+                 "build_o_matrix", "build_numerator"):
+        assert getattr(minimal, name) is getattr(pimc, name), name
