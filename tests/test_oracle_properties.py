@@ -1,7 +1,8 @@
 """A size-independent property of the reference algorithm, checked on the FP64 oracle (which the
 golden reference runs pin): the ring trace and rho's product are invariant under a cyclic
 relabelling of the beads, so every output -- rho, g, g(beta +- dbeta), scaled by the product of
-the per-bead S12 factors -- is unchanged when the beads of a sample are rotated."""
+the per-bead S12 factors -- is unchanged when the beads of a sample are rotated, and likewise when
+the ring is traversed backwards."""
 import numpy as np
 import pytest
 
@@ -16,5 +17,19 @@ def test_cyclic_bead_relabelling_leaves_outputs_unchanged(runs, name, shift):
     box = oracle_box_from_case(c, q.shape[2], X=6, B=6)
     a = box.evaluate(q)
     b = box.evaluate(np.roll(q, shift, axis=2))
+    for k in ("rho", "g", "gP", "gM"):
+        assert np.allclose(a[k], b[k], rtol=1e-11, atol=0), k
+
+
+@pytest.mark.parametrize("name", ["cfg2", "a8", "odd", "hot"])
+def test_reversed_bead_order_leaves_outputs_unchanged(runs, name):
+    """Reversing the ring maps each bead pair (p, p+1) to a pair of the reversed ring, so every O
+    and S12 factor reappears, and the reversed product is the transpose of the original one (M
+    and O are symmetric): its trace is unchanged."""
+    c = case_of(runs, name)
+    q = c["q"][:6]
+    box = oracle_box_from_case(c, q.shape[2], X=6, B=6)
+    a = box.evaluate(q)
+    b = box.evaluate(np.ascontiguousarray(q[..., ::-1]))
     for k in ("rho", "g", "gP", "gM"):
         assert np.allclose(a[k], b[k], rtol=1e-11, atol=0), k
