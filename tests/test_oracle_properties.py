@@ -33,3 +33,25 @@ def test_reversed_bead_order_leaves_outputs_unchanged(runs, name):
     b = box.evaluate(np.ascontiguousarray(q[..., ::-1]))
     for k in ("rho", "g", "gP", "gM"):
         assert np.allclose(a[k], b[k], rtol=1e-11, atol=0), k
+
+
+@pytest.mark.parametrize("name", ["cfg2", "odd", "a8"])
+def test_energy_shift_scales_the_ratios_exactly(runs, name):
+    """Shifting every diagonal energy of the coupled model by c moves into the O prefactors
+    (pimc.py:208-235, 1087-1129): g / rho scales by exp(-beta c) and g(beta +- dbeta) / rho by
+    exp(-(beta +- dbeta) c), per sample (the S12 scaling is common to numerator and denominator)."""
+    import json
+    from oracle import pimc_oracle as po
+    c = case_of(runs, name)
+    q = c["q"][:5]
+    P = q.shape[2]
+    beta, db = float(c["beta"]), float(c["delta_beta"])
+    T = 1.0 / (beta * po.KB_EV)
+    vib = json.loads(str(c["vib_json"]))
+    shift = 0.037
+    shifted = dict(vib, energies=(np.array(vib["energies"]) + shift * np.eye(len(vib["energies"]))).tolist())
+    rho = po.model_from_text(str(c["rho_json"]), diagonal=True)
+    a, b = (po.OracleBox(po.model_from_text(json.dumps(v)), rho, 5, 5, P, T, delta_beta=db,
+                         draw_sources=False).evaluate(q) for v in (vib, shifted))
+    for k, bk in (("g", beta), ("gP", beta + db), ("gM", beta - db)):
+        assert np.allclose((b[k] / b["rho"]) / (a[k] / a["rho"]), np.exp(-bk * shift), rtol=1e-11, atol=0), k
