@@ -55,3 +55,25 @@ def test_energy_shift_scales_the_ratios_exactly(runs, name):
                          draw_sources=False).evaluate(q) for v in (vib, shifted))
     for k, bk in (("g", beta), ("gP", beta + db), ("gM", beta - db)):
         assert np.allclose((b[k] / b["rho"]) / (a[k] / a["rho"]), np.exp(-bk * shift), rtol=1e-11, atol=0), k
+
+
+@pytest.mark.parametrize("name", ["cfg2", "odd"])
+def test_energy_shift_scaling_holds_in_the_kernel_formulation(runs, name):
+    """The same property for the kernel's own formulation (tests/kernel_model.py: the tables the
+    device uses, the beta series of order 4 for g(beta +- dbeta)), so the series carries the
+    exp(-(beta +- dbeta) c) factor to its truncation order."""
+    import json
+    import kernel_model
+    from conftest import prepared_from_case
+    c = case_of(runs, name)
+    q = c["q"][:5]
+    P = q.shape[2]
+    beta, db = float(c["beta"]), float(c["delta_beta"])
+    vib = json.loads(str(c["vib_json"]))
+    shift = 0.037
+    shifted = dict(c, vib_json=np.array(json.dumps(dict(
+        vib, energies=(np.array(vib["energies"]) + shift * np.eye(len(vib["energies"]))).tolist()))))
+    a = kernel_model.evaluate(prepared_from_case(c, P), q)
+    b = kernel_model.evaluate(prepared_from_case(shifted, P), q)
+    for k, bk in (("s_g", beta), ("s_gp", beta + db), ("s_gm", beta - db)):
+        assert np.allclose((b[k] / b["s_rho"]) / (a[k] / a["s_rho"]), np.exp(-bk * shift), rtol=1e-11, atol=0), k
