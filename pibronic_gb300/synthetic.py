@@ -45,6 +45,30 @@ def make_coupled_model(A, N, seed, sd_offdiag=0.05, sd_linear=0.01, sd_quadratic
     return {VMK.N: N, VMK.A: A, VMK.E: E, VMK.w: w, VMK.G1: L, VMK.G2: Q}
 
 
+def make_near_degenerate_model(A, N, seed, eps=1e-7, sd_quadratic=0.002):
+    """A coupled model whose surfaces are degenerate up to couplings of size eps (eV): every
+    surface has the same energy, linear and quadratic diagonal terms (those of surface 0 of the
+    recipe above), and the off-diagonal energies, linear and quadratic couplings are N(0, eps).
+    V(q) is then v0(q) I + O(eps) at every q: its eigenvalues coincide to ~eps and its eigenvectors
+    are ill-conditioned, while exp(-tau V) is not (the reference forms it with LAPACK eigh,
+    pimc.py:1171-1173)."""
+    base = make_coupled_model(A, N, seed, sd_quadratic=sd_quadratic)
+    rng = np.random.default_rng(seed + 7)
+    eye = np.eye(A)
+
+    def sym_noise(shape):
+        x = rng.normal(0.0, eps, size=shape)
+        x = 0.5 * (x + np.swapaxes(x, -1, -2))
+        return x * (1.0 - eye)
+
+    E = base[VMK.E][0, 0] * eye + sym_noise((A, A))
+    L = base[VMK.G1][:, 0, 0][:, None, None] * eye + sym_noise((N, A, A))
+    Qn = sym_noise((N, N, A, A))
+    Qn = 0.5 * (Qn + Qn.transpose(1, 0, 2, 3))
+    Q = base[VMK.G2][:, :, 0, 0][:, :, None, None] * eye + Qn
+    return {VMK.N: N, VMK.A: A, VMK.E: E, VMK.w: base[VMK.w], VMK.G1: L, VMK.G2: Q}
+
+
 def diagonal_of(model):
     out = {VMK.N: model[VMK.N], VMK.A: model[VMK.A]}
     for key in (VMK.E, VMK.w, VMK.G1, VMK.G2):

@@ -1,8 +1,11 @@
 """Generate the golden fixtures under tests/golden/ from the reference implementation itself.
 
-Run in a container where the reference is mounted (default /root/reference):
+Run where a checkout of the reference is available:
 
-    python tests/golden/make_golden.py [path_to_reference]
+    python tests/golden/make_golden.py PATH_TO_REFERENCE [--cases NAME,NAME]
+    PIBRONIC_REFERENCE=PATH_TO_REFERENCE python tests/golden/make_golden.py
+
+With --cases only the named seeded cases are (re)run and merged into reference_runs.npz.
 
 It (1) packs the reference's own known-answer data (tests/pimc/explicit_data/*) into
 explicit_example.npz, and (2) imports the unmodified reference engine from a temporary copy
@@ -131,9 +134,13 @@ def write_models(root, case):
     if "vib_json" in case:
         vib_text, rho_text = case["vib_json"], case["rho_json"]
     else:
-        model = synthetic.make_coupled_model(case["A"], case["N"], case["model_seed"],
-                                             sd_offdiag=case.get("sd_offdiag", 0.05),
-                                             sd_quadratic=case.get("sd_quadratic", 0.002))
+        if case.get("degenerate"):
+            model = synthetic.make_near_degenerate_model(case["A"], case["N"], case["model_seed"],
+                                                         eps=case["degenerate"])
+        else:
+            model = synthetic.make_coupled_model(case["A"], case["N"], case["model_seed"],
+                                                 sd_offdiag=case.get("sd_offdiag", 0.05),
+                                                 sd_quadratic=case.get("sd_quadratic", 0.002))
         if case.get("zero_diag_linear"):
             # equal state shifts keep V symmetric when each surface slot holds R - d_a
             # (the learned-proposal data path asserts that symmetry, pimc.py:1169)
@@ -445,10 +452,38 @@ CASES = {
     # hot (1000 K, short tau) and cold (50 K, long tau) ends of the temperature range
     "hot": dict(A=3, N=4, P=16, T=1000.0, X=30, B=15, model_seed=1000, rng_seed=1001),
     "frozen": dict(A=2, N=3, P=32, T=50.0, X=20, B=10, model_seed=50, rng_seed=51),
+    # the main benchmark shapes at the high temperature of their sweep (500 K)
+    "cfg2_hot": dict(A=4, N=12, P=64, T=500.0, X=40, B=20, model_seed=25, rng_seed=505),
+    # near-degenerate surfaces: equal diagonal terms, off-diagonal couplings ~ 1e-7 eV (two
+    # surfaces: the Jacobi rotation; four: the scaling-and-squaring exponential; seven: the
+    # row-team form's Jacobi; twelve: the wide form on the tensor-core potential)
+    "degen2": dict(A=2, N=3, P=16, T=300.0, X=30, B=15, model_seed=72, rng_seed=721, degenerate=1e-7),
+    "degen4": dict(A=4, N=6, P=32, T=300.0, X=30, B=15, model_seed=74, rng_seed=741, degenerate=1e-7),
+    "degen7": dict(A=7, N=3, P=8, T=300.0, X=21, B=7, model_seed=77, rng_seed=771, degenerate=1e-7),
+    "degen12": dict(A=12, N=4, P=8, T=300.0, X=12, B=6, model_seed=712, rng_seed=7121, degenerate=1e-7),
 }
 
 
-def main(ref_root="/root/reference"):
+def add_cases(ref_root, names):
+    """Run only the named CASES through the reference and merge them into reference_runs.npz
+    (every other fixture and entry is left as it is)."""
+    engine, st, jk, fs, const, tmp = import_reference(ref_root)
+    path = os.path.join(HERE, "reference_runs.npz")
+    with np.load(path) as d:
+        runs = {k: d[k] for k in d.files}
+    for name in names:
+        runs = {k: v for k, v in runs.items() if not k.startswith(name + "/")}
+        out = run_case(engine, fs, const, CASES[name])
+        for k, v in out.items():
+            runs[f"{name}/{k}"] = v
+        print(name, {k: np.shape(v) for k, v in out.items()})
+    np.savez_compressed(path, **runs)
+    with open(os.path.join(HERE, "cases.json"), "w") as fh:
+        json.dump(CASES, fh, indent=1)
+    shutil.rmtree(tmp, ignore_errors=True)
+
+
+def main(ref_root):
     keys = explicit_example(ref_root)
     print("explicit_example.npz:", keys)
     print("reference_sos_results.npz:", sos_results(ref_root))
@@ -497,4 +532,16 @@ def main(ref_root="/root/reference"):
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("reference", nargs="?", default=os.environ.get("PIBRONIC_REFERENCE"),
+                    help="root of the reference checkout (or set PIBRONIC_REFERENCE)")
+    ap.add_argument("--cases", default="", help="comma-separated CASES to (re)run and merge into "
+                    "reference_runs.npz, leaving every other fixture as it is")
+    a = ap.parse_args()
+    if not a.reference:
+        ap.error("give the reference checkout's root (argument or PIBRONIC_REFERENCE)")
+    if a.cases:
+        add_cases(a.reference, [c for c in a.cases.split(",") if c])
+    else:
+        main(a.reference)

@@ -5,8 +5,11 @@ Tolerances (stated per output):
   * FP64 validation kernels (precision=64): rtol 1e-9 on rho, g, g(beta +- db) -- the algorithm
     itself, bit-for-bit up to rounding (the reference's own O exponent carries ~1e-12 rounding).
   * FP32 production kernel: rtol 2e-4 on rho, g, g(beta +- db); the finite-difference terms
-    s1 = (g+ - g-)/(2 db rho) rtol 2e-3; s2 = (g+ - 2g + g-)/(db^2 rho) within 2e-2 of max|s2|
-    (per sample; they are reductions of ~1e-3 .. 1e-5 relative differences of g).
+    s1 = (g+ - g-)/(2 db rho) rtol 2e-3; s2 = (g+ - 2g + g-)/(db^2 rho) within 2e-4 of max|s2|
+    per sample (measured on GB300: at most 6.2e-5, on the reference's test model; 1e-7 .. 2e-5
+    on the synthetic cases).  The kernel forms g+- from one ring product of series in beta, so
+    the FP32 rounding of g, g+ and g- is shared and s2 does not inherit the cancellation of
+    g+ - 2g + g-.
   * Stage kernels (FP64): the reference test's rtol 1e-5, atol 1e-8.
 """
 import numpy as np
@@ -18,9 +21,9 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel",
-         "cfg4", "a8", "a7"]
-WIDE = {"cfg4", "a8", "a7"}                       # A > 4: the row-team form only
+CASES = ["cfg1", "cfg2", "cfg2_cold", "cfg2_hot", "odd", "plain", "arho", "single_surface",
+         "testmodel", "cfg4", "a8", "a7", "p3_n1", "hot", "frozen", "degen2", "degen4", "degen7"]
+WIDE = {"cfg4", "a8", "a7", "degen7"}             # A > 4: the row-team form only
 # (case, kernel form): 1 = register-resident chunks, 2 = bead-parallel records + row teams
 FORMS = [(c, v) for c in CASES for v in (1, 2) if not (v == 1 and c in WIDE)]
 
@@ -71,7 +74,9 @@ def test_fused_fp32_matches_reference(runs, name, variant):
         assert np.allclose(s1, s1r, rtol=2e-3, atol=1e-6 * np.abs(s1r).max())
         s2r = (c["s_gP"] - 2 * c["s_g"] + c["s_gM"]) / (db ** 2 * c["s_rho"])
         s2 = (got["s_gp"] - 2 * got["s_g"] + got["s_gm"]) / (db ** 2 * got["s_rho"])
-        assert np.max(np.abs(s2 - s2r)) <= 2e-2 * np.abs(s2r).max()
+        err = np.max(np.abs(s2 - s2r)) / np.abs(s2r).max()
+        print(f"{name} form {variant}: s2 max error {err:.2e} of max|s2|")
+        assert err <= 2e-4, err
 
 
 def test_fp32_q_input_matches_fp64_q_input(runs):
@@ -164,7 +169,7 @@ def test_stage_scaling_matches_oracle(runs):
     assert np.allclose(y_g, ref["g"], rtol=1e-9)
 
 
-@pytest.mark.parametrize("name", ["a12", "a16", "a8"])
+@pytest.mark.parametrize("name", ["a12", "a16", "a8", "degen12", "degen7", "degen4"])
 def test_tensor_core_form_matches_reference(runs, name):
     """The tensor-core form (V(q) by the tcgen05 GEMM; the wide kernel above 8 surfaces, the
     row-team kernel on the GEMM's V up to 8) on the reference's recorded q, against the

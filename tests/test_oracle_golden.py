@@ -75,7 +75,8 @@ def test_explicit_block_compute(ex_box, explicit):
 
 
 CASES = ["cfg1", "cfg2", "cfg2_cold", "odd", "plain", "arho", "single_surface", "testmodel",
-         "cfg4", "a8", "a7", "a12", "a16", "p3_n1", "hot", "frozen"]
+         "cfg4", "a8", "a7", "a12", "a16", "p3_n1", "hot", "frozen", "cfg2_hot", "degen2",
+         "degen4", "degen7", "degen12"]
 
 
 @pytest.mark.parametrize("name", CASES)
