@@ -603,7 +603,9 @@ def large_leg(args):
     useful = 2.0 * Xc * P * (A * (A + 1) // 2) * (N * (N + 1) // 2 + N + 1) / t_tc / 1e12
     peak = tf32_cublas_peak(torch)
     rate, cyc = ctypes.c_double(), ctypes.c_double()
-    _native.check(lib.pbr_tc_mma_rate(128, 256, 4096, ctypes.byref(rate), ctypes.byref(cyc), sh), "mma rate")
+    probe = torch.empty(2, dtype=torch.float64, device="cuda")
+    _native.check(lib.pbr_tc_mma_rate(128, 256, 4096, _native.ptr(probe), ctypes.byref(rate), ctypes.byref(cyc), sh),
+                  "mma rate")
 
     def summary(e, t):
         rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
@@ -674,6 +676,31 @@ def profile_large(args):
     return 0
 
 
+def profile_learned(args):
+    """Profiling helper (no timing, no JSON line): two plain-rho evaluations of args.profile_learned
+    samples of the learned-proposal configuration's model (A=6, N=20, P=128, T=200 K, strong
+    couplings; the row-team form), for an ncu capture."""
+    import torch
+    from pibronic_gb300 import constants, pimc, synthetic
+    from pibronic_gb300.file_structure import FileStructure
+    from pibronic_gb300.pimc import evaluate_device
+    A, N, P, T = 6, 20, 128, 200.0
+    FS = FileStructure(tempfile.mkdtemp(prefix="pbr_plearn_"), 0, 0)
+    synthetic.write_model_pair(FS, A, N, args.learned_seeds[0], sd_offdiag=0.1)
+    data = pimc.BoxDataPM(1e-4 * constants.beta(T))
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.states, data.modes, data.beads, data.temperature = A, N, P, T
+    data.samples = data.block_size = 1000
+    data.blocks = 1
+    data.preprocess()
+    for i in range(2):
+        out = evaluate_device(data.plan, args.profile_learned, seed=1 + i, offset=0)
+    torch.cuda.synchronize()
+    assert int(out["status"].item()) == 0
+    print("profile-learned done", args.profile_learned)
+    return 0
+
+
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
     each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
@@ -722,9 +749,14 @@ def main():
     ap.add_argument("--large-samples", type=int, default=400_000)
     ap.add_argument("--profile-large", type=int, default=0,
                     help="profiling helper: evaluate this many samples of the large configuration twice, exit")
+    ap.add_argument("--profile-learned", type=int, default=0,
+                    help="profiling helper: evaluate this many plain-rho samples of the learned "
+                         "configuration's model twice, exit")
     args = ap.parse_args()
     if args.profile_large > 0:
         return profile_large(args)
+    if args.profile_learned > 0:
+        return profile_learned(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -143,7 +143,8 @@ int pbr_eval_q_tc(const pbr_model* model, const float* q, int64_t X, const pbr_o
  * Many independent models in one launch per surface count (the batched configuration): every
  * model keeps its own sizes, temperature, seed, counter offset and outputs.  pbr_batch_pack fills
  * a host blob of pbr_batch_blob_bytes(n) bytes (tile shapes per model within smem_budget bytes of
- * shared memory, 0 = the maximum; models grouped by surface count and series order; grid_cap
+ * shared memory, 0 = the maximum; a model whose one-sample tile exceeds the budget takes the
+ * maximum instead; models grouped by surface count and series order; grid_cap
  * limits the persistent grid, 0 = occupancy x SMs); the caller copies it to a device buffer of the
  * same size; pbr_sample_eval_batch launches one persistent row-team kernel per group, CTAs taking
  * the concatenated tiles round-robin, except that groups of up to 4 surfaces (whose models all
@@ -194,6 +195,11 @@ int pbr_o_matrix(const double* q_slots, int64_t B, int32_t Am, int32_t N, int32_
  * Replaces build_scaling_factors + scale_o_matrices (pimc.py:1062-1084, 1443, 1448). */
 int pbr_scale_o_matrices(double* O1, int32_t A1, double* O2, int32_t A2, int64_t B, int32_t P,
                          double* S12, void* stream);
+
+/* S1[B,P] = max over O1[b,p], S2[B,P] = max over O2[b,p] (S1, S2 nullable), S12 = max(S1, S2).
+ * Replaces build_scaling_factors (pimc.py:1076-1084). */
+int pbr_scaling_factors(const double* O1, int32_t A1, const double* O2, int32_t A2, int64_t B, int32_t P,
+                        double* S1, double* S2, double* S12, void* stream);
 
 /* O[B,P,A,A] /= S12[B,P] (pimc.py:1443). */
 int pbr_divide_o_matrix(double* O, int32_t A, int64_t B, int32_t P, const double* S12,
@@ -272,7 +278,10 @@ int64_t pbr_reduce_blocks(int64_t X);
  * X <= pbr_reduce_terms_static_max_samples() = 4,194,304; larger X returns PBR_ERR_CAPACITY and
  * launches nothing.  Results equal pbr_reduce_terms's for the same inputs.  The first call on a
  * device looks the array's device address up (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the one array: calls that
+ * make that first call before any stream capture.  The address is kept for the life of the
+ * process: a cudaDeviceReset (or any release and re-creation of the device's primary context)
+ * can move the array, so after one this entry point must not be called again on that device in
+ * the same process.  All calls share the one array: calls that
  * overlap on the GPU (other streams, other host threads) race and must be serialised by the
  * caller.
  */
@@ -394,9 +403,11 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
  */
 /* Tensor-pipe rate: one CTA per SM issues reps back-to-back tcgen05.mma kind::tf32 (M x N x 8,
  * M 64 or 128, 16 <= N <= 256) from one thread; *tflops is the whole-GPU rate, *cycles_per_mma the
- * issuing thread's cycles per instruction.  Allocates and frees two small device buffers (a
- * measurement, not a path entry point).  No counterpart in the reference. */
-int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, double* tflops, double* cycles_per_mma, void* stream);
+ * issuing thread's cycles per instruction.  scratch: 16 bytes of the caller's device memory,
+ * 8-byte aligned (the cycle count and the kernel's wait flag).  Synchronizes the stream to read the
+ * result (a measurement, not a path entry point).  No counterpart in the reference. */
+int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch, double* tflops, double* cycles_per_mma,
+                    void* stream);
 
 int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
 int64_t pbr_tc_potential_packed_floats(int32_t N, int32_t A);

@@ -25,7 +25,7 @@ _STATUS_TEXT = {
 #: every symbol declared in include/pibronic_gb300.h
 EXPORTED = (
     "pbr_sample_eval", "pbr_sample_q", "pbr_eval_q", "pbr_eval_q_f32",
-    "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_divide_o_matrix", "pbr_denominator",
+    "pbr_o_matrix", "pbr_scale_o_matrices", "pbr_scaling_factors", "pbr_divide_o_matrix", "pbr_denominator",
     "pbr_coupling_eigh", "pbr_numerator",
     "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_fma_probe",
     "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples",
@@ -89,6 +89,7 @@ def _declare(lib):
         "pbr_eval_q_f32": (C.c_int, [C.POINTER(PbrModel), vp, i64, C.POINTER(PbrOutputs), vp]),
         "pbr_o_matrix": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, i32, vp, vp]),
         "pbr_scale_o_matrices": (C.c_int, [vp, i32, vp, i32, i64, i32, vp, vp]),
+        "pbr_scaling_factors": (C.c_int, [vp, i32, vp, i32, i64, i32, vp, vp, vp, vp]),
         "pbr_divide_o_matrix": (C.c_int, [vp, i32, i64, i32, vp, vp]),
         "pbr_denominator": (C.c_int, [vp, i64, i32, i32, vp, vp]),
         "pbr_coupling_eigh": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -121,7 +122,7 @@ def _declare(lib):
         "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
         "pbr_tc_potential_packed_floats": (i64, [i32, i32]),
-        "pbr_tc_mma_rate": (C.c_int, [i32, i32, i32, C.POINTER(f64), C.POINTER(f64), vp]),
+        "pbr_tc_mma_rate": (C.c_int, [i32, i32, i32, vp, C.POINTER(f64), C.POINTER(f64), vp]),
         "pbr_tc_pack_potential": (C.c_int, [vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp]),
         "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),

@@ -296,7 +296,11 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
                     (K > 0 && (!outs[i].s_gp || !outs[i].s_gm)) || !m.ring_chol || !m.src_cdf)
                     return PBR_ERR_ARG;
                 TeamArgs a;
-                const int rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], budget, &a);
+                int rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], budget, &a);
+                // a model whose one-sample tile does not fit the budget takes the full shared
+                // memory instead of vetoing the budget for the whole batch
+                if (rc == PBR_ERR_UNSUPPORTED && budget < kMaxSmem)
+                    rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], kMaxSmem, &a);
                 if (rc != PBR_OK) return rc;
                 const bool two = (A == 5 || A == 6) && team_smem(a, kSample) <= kTeamTwoBlockSmem;
                 if ((cls == 0) != two) continue;

@@ -332,9 +332,11 @@ static __device__ __align__(256) double g_static_scratch[kStaticScratchDoubles];
 std::mutex g_static_mutex;
 double* g_static_addr[kMaxDevices] = {nullptr};
 
-// Device address of g_static_scratch on the current device, looked up once per device.  In
-// host code the symbol name is only a host-side stand-in for the array, so kernels must be given
-// this address, never &g_static_scratch.
+// Device address of g_static_scratch on the current device, looked up once per device and kept
+// for the life of the process (a device reset that re-creates the context can move the array; the
+// header tells callers not to use this entry point on a device after one).  In host code the
+// symbol name is only a host-side stand-in for the array, so kernels must be given this address,
+// never &g_static_scratch.
 int static_scratch_address(double** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return PBR_ERR_CUDA;

@@ -54,6 +54,21 @@ __global__ void scale_kernel(double* O1, int A1, double* O2, int A2, int64_t BP,
     S12[idx] = mx;
 }
 
+// per (sample, bead): each model's max O entry and the larger of the two (pimc.py:1076-1084)
+__global__ void scaling_factors_kernel(const double* O1, int A1, const double* O2, int A2, int64_t BP,
+                                       double* S1, double* S2, double* S12) {
+    const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= BP) return;
+    const double* b1 = O1 + idx * A1 * A1;
+    const double* b2 = O2 + idx * A2 * A2;
+    double m1 = b1[0], m2 = b2[0];
+    for (int i = 1; i < A1 * A1; ++i) m1 = fmax(m1, b1[i]);
+    for (int i = 1; i < A2 * A2; ++i) m2 = fmax(m2, b2[i]);
+    if (S1) S1[idx] = m1;
+    if (S2) S2[idx] = m2;
+    S12[idx] = fmax(m1, m2);
+}
+
 __global__ void divide_kernel(double* O, int A, int64_t BP, const double* S12) {
     const int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (idx >= BP) return;
@@ -241,6 +256,15 @@ int pbr_scale_o_matrices(double* O1, int32_t A1, double* O2, int32_t A2, int64_t
     if (B == 0) return PBR_OK;
     scale_kernel<<<grid_for(B * P), kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(
         O1, A1, O2, A2, B * P, S12);
+    return last_status();
+}
+
+int pbr_scaling_factors(const double* O1, int32_t A1, const double* O2, int32_t A2, int64_t B, int32_t P,
+                        double* S1, double* S2, double* S12, void* stream) {
+    if (!O1 || !O2 || !S12 || A1 < 1 || A2 < 1 || B < 0 || P < 1) return PBR_ERR_ARG;
+    if (B == 0) return PBR_OK;
+    scaling_factors_kernel<<<grid_for(B * P), kStageThreads, 0, static_cast<cudaStream_t>(stream)>>>(
+        O1, A1, O2, A2, B * P, S1, S2, S12);
     return last_status();
 }
 

@@ -789,10 +789,10 @@ __global__ void tc_rate_kernel(int M, int N, int reps, int32_t* flag, long long*
 
 }  // namespace
 
-extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, double* tflops, double* cycles_per_mma,
-                               void* stream) {
+extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch, double* tflops,
+                               double* cycles_per_mma, void* stream) {
     if ((M != 64 && M != 128) || N < 16 || N > 256 || N % 16 != 0 || reps < 1 || reps > (1 << 20) || !tflops ||
-        !cycles_per_mma)
+        !cycles_per_mma || !scratch || (reinterpret_cast<uintptr_t>(scratch) & 7) != 0)
         return PBR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int dev = 0, sms = 0;
@@ -801,34 +801,32 @@ extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, double* tflop
     constexpr int kSmem = 120 * 1024;      // one CTA per SM
     if (cudaFuncSetAttribute(tc_rate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem) != cudaSuccess)
         return PBR_ERR_UNSUPPORTED;
-    int32_t* dflag = nullptr;
-    long long* dcyc = nullptr;
-    PBR_CUDA_CHECK_RET(cudaMalloc(&dflag, sizeof(int32_t)));
-    PBR_CUDA_CHECK_RET(cudaMalloc(&dcyc, sizeof(long long)));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
+    // the caller's 16 bytes: the cycle count (8-byte aligned) and the bounded-wait flag after it
+    long long* dcyc = static_cast<long long*>(scratch);
+    int32_t* dflag = reinterpret_cast<int32_t*>(static_cast<char*>(scratch) + 8);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     int rc = PBR_OK;
-    cudaMemsetAsync(dflag, 0, sizeof(int32_t), st);
-    tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, 64, dflag, dcyc);        // warm-up
-    cudaEventRecord(e0, st);
-    tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, reps, dflag, dcyc);
-    cudaEventRecord(e1, st);
-    if (cudaEventSynchronize(e1) != cudaSuccess) rc = PBR_ERR_CUDA;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = PBR_ERR_CUDA;
+    if (rc == PBR_OK && cudaMemsetAsync(scratch, 0, 16, st) != cudaSuccess) rc = PBR_ERR_CUDA;
+    if (rc == PBR_OK) {
+        tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, 64, dflag, dcyc);        // warm-up
+        cudaEventRecord(e0, st);
+        tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, reps, dflag, dcyc);
+        cudaEventRecord(e1, st);
+        if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) rc = PBR_ERR_CUDA;
+    }
     float ms = 0.f;
     long long cyc = 0;
     int32_t flag = 0;
-    if (rc == PBR_OK) {
-        cudaEventElapsedTime(&ms, e0, e1);
-        cudaMemcpy(&cyc, dcyc, sizeof(cyc), cudaMemcpyDeviceToHost);
-        cudaMemcpy(&flag, dflag, sizeof(flag), cudaMemcpyDeviceToHost);
-        if (flag) rc = PBR_ERR_CUDA;
-    }
-    *tflops = (ms > 0.f) ? 2.0 * M * N * 8.0 * reps * sms / (ms * 1e-3) / 1e12 : 0.0;
-    *cycles_per_mma = static_cast<double>(cyc) / reps;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(dflag);
-    cudaFree(dcyc);
+    if (rc == PBR_OK && (cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess ||
+                         cudaMemcpyAsync(&cyc, dcyc, sizeof(cyc), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                         cudaMemcpyAsync(&flag, dflag, sizeof(flag), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                         cudaStreamSynchronize(st) != cudaSuccess))
+        rc = PBR_ERR_CUDA;
+    if (rc == PBR_OK && flag) rc = PBR_ERR_CUDA;      // a wait in the kernel gave up
+    *tflops = (rc == PBR_OK && ms > 0.f) ? 2.0 * M * N * 8.0 * reps * sms / (ms * 1e-3) / 1e12 : 0.0;
+    *cycles_per_mma = rc == PBR_OK ? static_cast<double>(cyc) / reps : 0.0;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
     return rc;
 }

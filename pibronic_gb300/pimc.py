@@ -593,10 +593,21 @@ def build_o_matrix(data, model, state_shift):
 
 
 def build_scaling_factors(S12, model_one, model_two):
-    """S12 = max of both models' O per (sample, bead) (pimc.py:1076-1084)."""
-    model_one.omatrix_scaling = model_one.omatrix.amax(dim=(2, 3))
-    model_two.omatrix_scaling = model_two.omatrix.amax(dim=(2, 3))
-    s = _torch().maximum(model_one.omatrix_scaling, model_two.omatrix_scaling)
+    """Each model's max O entry per (sample, bead) and S12, the larger of the two
+    (pimc.py:1076-1084), by the library's pbr_scaling_factors."""
+    torch = _torch()
+    lib = _native.load()
+    O1, O2 = model_one.omatrix, model_two.omatrix
+    B, P, A1, _ = O1.shape
+    A2 = O2.shape[2]
+    assert O2.shape[:2] == (B, P), "both models' O matrices must cover the same samples and beads"
+    model_one.omatrix_scaling = torch.empty((B, P), dtype=torch.float64, device="cuda")
+    model_two.omatrix_scaling = torch.empty((B, P), dtype=torch.float64, device="cuda")
+    s = torch.empty((B, P), dtype=torch.float64, device="cuda")
+    _native.check(lib.pbr_scaling_factors(_native.ptr(O1), A1, _native.ptr(O2), A2, B, P,
+                                          _native.ptr(model_one.omatrix_scaling),
+                                          _native.ptr(model_two.omatrix_scaling), _native.ptr(s),
+                                          _native.stream_handle()), "build_scaling_factors")
     if hasattr(S12, "copy_"):
         S12.copy_(s)
     else:
