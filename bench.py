@@ -228,8 +228,20 @@ def fp32_peak(torch, lib, stream):
     return best
 
 
+def measured_hbm_gbs():
+    """(HBM copy bandwidth in GB/s, where it came from): the pool's measured figure when
+    MEASURED_PEAKS.json is present, else the fallback of one earlier GB300 measurement."""
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
 def read_traffic():
-    """DRAM bytes per fused launch from the committed ncu summary, if present."""
+    """DRAM bytes (read + write) of one 1e6-sample fused launch, measured by ncu on this bench's
+    own command (the launch list in profiles/fused_config2_ncu.md), if that summary is present."""
     path = os.path.join(HERE, "profiles", "fused_config2_ncu.md")
     if not os.path.exists(path):
         return None
@@ -344,7 +356,10 @@ def run_ours(args):
         ess_total = statistics.mean(e["ESS"] for e in ests)
     value = ess_total / (ms_step * 1e-3)
     sps = X * world / (ms_step * 1e-3)
-    e = ests[-1]
+    # the last step's estimates over all ranks' samples: moments merged in rank order and the
+    # jackknife pass of every rank against the global totals (after the timed region)
+    e = red.pooled(bufs["s_rho"], bufs["s_g"], bufs["s_gp"], bufs["s_gm"], data.delta_beta, T_) if dist \
+        else ests[-1]
     rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
            "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
     t_1e3 = {k: X * world * (v / 1e-3) ** 2 / sps for k, v in rel.items()}
@@ -413,24 +428,31 @@ def run_ours(args):
     achieved = W * X / (ms_kern * 1e-3) / 1e12
     peak = fp32_peak(torch, lib, stream)
     traffic = read_traffic()
+    hbm = measured_hbm_gbs()
     roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one 1e6-sample launch "
+                              "of this command (profiles/fused_config2_ncu.md); the outputs stay in L2",
+            "algorithmic_bytes": 32 * X,
             "peak_source": "FP32 FFMA probe (pbr_fma_probe) measured in this run; "
                            "MEASURED_PEAKS.json has only HBM copy and bf16 tensor peaks",
             "flops_per_sample": W, "kernel_ms": ms_kern,
-            "hbm_frac_of_measured": (32.0 * X / (ms_kern * 1e-3) / 1e9) / 6801.7}
+            "hbm_frac_of_measured": (32.0 * X / (ms_kern * 1e-3) / 1e9) / hbm[0], "hbm_peak_source": hbm[1]}
     line = {
         "metric": METRIC, "value": value, "unit": "ESS/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
         "samples_per_s": sps, "ess_per_sample": ess_total / (X * world),
-        "rel_err": rel, "time_to_1e-3_s": t_1e3,
+        "rel_err": rel, "time_to_1e-3_s": t_1e3, "estimates_over": f"{world} rank(s), {X * world} samples",
         "estimates": {k: e[k] for k in ("Z", "Z error", "E", "jk_E", "jk_E error", "Cv", "jk_Cv", "jk_Cv error")},
         "roofline": roof,
         "e2e": {"value": e2e_val, "unit": "ESS/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "ms_per_step": 1e3 * e2e_t},
         "clocks": clk, "gpu_launches": 5 * args.steps,
     }
+    # ---- FP32 against the FP64 build on identical q at 100, 300, 500 K ----
+    if rank == 0 and not args.no_precision:
+        line["precision"] = precision_leg(args)
     # ---- learned proposal vs plain rho (A=6, N=20, P=128, T=200 K, strong couplings) ----
     if rank == 0 and not args.no_learned:
         line["learned"] = learned_leg(args)
@@ -473,19 +495,49 @@ def _warm_training(torch, FlowProposal, prepared, plan, nsel, y, r):
     torch.cuda.synchronize()
 
 
+def rate_summary(e, t, X, train_s=0.0):
+    """ESS/s, samples/s, estimates and the wall time to 1e-3 relative error of Z, E and Cv at the
+    measured rate (X (rel / 1e-3)^2 samples), plus train_s when given.  A quantity within 3 of its
+    statistical errors of zero has no meaningful relative error: its time is None."""
+    out = {"samples": X, "ess_per_sample": e["ESS"] / X, "ess_per_s": e["ESS"] / t, "samples_per_s": X / t,
+           "Z": e["Z"], "Z error": e["Z error"], "E": e["jk_E"], "E error": e["jk_E error"],
+           "Cv": e["jk_Cv"], "Cv error": e["jk_Cv error"]}
+    times = {}
+    for k, v, err in (("Z", e["Z"], e["Z error"]), ("E", e["jk_E"], e["jk_E error"]),
+                      ("Cv", e["jk_Cv"], e["jk_Cv error"])):
+        times[k] = None if abs(v) < 3.0 * err else train_s + X * (err / abs(v) / 1e-3) ** 2 / (X / t)
+    out["time_to_1e-3_s"] = times
+    return out
+
+
+def _chunked(torch, fn, X, chunk):
+    """Run fn(n, offset) over X samples in chunks; returns (concatenated outputs, seconds)."""
+    outs = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for off in range(0, X, chunk):
+        outs.append(fn(min(chunk, X - off), off))
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    keys = ("s_rho", "s_q", "s_g", "s_gp", "s_gm")
+    return {k: torch.cat([o[k] for o in outs]) for k in keys if k in outs[0]}, t
+
+
 def learned_leg(args):
-    """The learned-proposal configuration: plain rho vs the affine-coupling flow trained on 2e6 of
-    rho's own weighted samples plus one round on its own samples; ESS/s includes the flow's
-    sampling and evaluation, training time is reported separately."""
+    """The learned-proposal configuration: plain rho vs the affine-coupling flow, each evaluated on
+    args.learned_samples samples (1e7).  The flow is trained on 2e6 of rho's own weighted samples
+    plus one round on 1e6 of its own; its training cost (drawing those samples and the two training
+    rounds) is reported and added to its wall time to 1e-3."""
     import torch
     from pibronic_gb300 import constants, pimc, stats, synthetic
     from pibronic_gb300.file_structure import FileStructure
     from pibronic_gb300.flow import FlowProposal
     from pibronic_gb300.pimc import evaluate_device
     A, N, P, T = 6, 20, 128, 200.0
-    X = args.learned_samples
+    X, C = args.learned_samples, 1_000_000
     out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K off-diagonal couplings N(0,0.1) eV, dbeta=1e-4 beta, "
-                       f"{X} samples per evaluation; flow: 8 coupling layers, hidden 128, 3 ring slots per mode",
+                       f"{X} samples per estimate; flow: 8 coupling layers, hidden 128, 3 ring slots per mode, "
+                       f"trained on 2e6 rho samples + 1e6 of its own",
            "models": []}
     for seed in args.learned_seeds:
         root = tempfile.mkdtemp(prefix="pbr_learned_")
@@ -498,38 +550,47 @@ def learned_leg(args):
         data.blocks = 1
         data.preprocess()
         evaluate_device(data.plan, 10_000, seed=99, offset=0)
-        plain, tp = _timed(torch, lambda: evaluate_device(data.plan, X, seed=1, offset=0, want_q=True))
-        ep = stats.device_estimates(plain["s_rho"], plain["s_g"], plain["s_gp"], plain["s_gm"], T, data.delta_beta)
         fl = FlowProposal(data.prepared, data.plan, nsel=3, layers=8, hidden=128, seed=0)
+        # ---- training cost: rho's samples with their q, two training rounds ----
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
         ys, rs = [], []
-        for k, pl in enumerate((plain, evaluate_device(data.plan, X, seed=1, offset=X, want_q=True))):
+        for k in range(2):
+            pl = evaluate_device(data.plan, C, seed=1001, offset=k * C, want_q=True)
             y, _ = fl.prepare(pl["q"])
             ys.append(y)
             rs.append(pl["s_g"] / pl["s_rho"])
-            del pl["q"]
-        _warm_training(torch, FlowProposal, data.prepared, data.plan, 3, ys[0], rs[0])
-        _, t_train = _timed(torch, lambda: fl.train(torch.cat(ys), torch.cat(rs), epochs=6, batch=16384, lr=1e-3))
-        first = fl.sample_and_evaluate(X, seed=7, keep=True)
-        _, t2 = _timed(torch, lambda: fl.train(first["y"], first["s_g"] / first["s_q"], epochs=6, batch=16384,
-                                               lr=1e-3))
+            del pl
+        torch.cuda.synchronize()
+        t_draw = time.perf_counter() - t0
+        if not out["models"]:
+            _warm_training(torch, FlowProposal, data.prepared, data.plan, 3, ys[0], rs[0])
+        _, t_train1 = _timed(torch, lambda: fl.train(torch.cat(ys), torch.cat(rs), epochs=6, batch=16384, lr=1e-3))
+        del ys, rs
+        first, t_own = _timed(torch, lambda: fl.sample_and_evaluate(C, seed=7, keep=True))
+        _, t_train2 = _timed(torch, lambda: fl.train(first["y"], first["s_g"] / first["s_q"], epochs=6,
+                                                     batch=16384, lr=1e-3))
         del first
+        train_s = t_draw + t_train1 + t_own + t_train2
+        # ---- the two estimates, X samples each ----
         fl.sample_and_evaluate(10_000, seed=5)
-        res, tf = _timed(torch, lambda: fl.sample_and_evaluate(X, seed=8))
+        plain, tp = _chunked(torch, lambda n, off: evaluate_device(data.plan, n, seed=1, offset=off), X, C)
+        ep = stats.device_estimates(plain["s_rho"], plain["s_g"], plain["s_gp"], plain["s_gm"], T, data.delta_beta)
+        del plain
+        res, tf = _chunked(torch, lambda n, off: fl.sample_and_evaluate(n, seed=8, offset=off), X, C)
         ef = stats.device_estimates(res["s_q"], res["s_g"], res["s_gp"], res["s_gm"], T, data.delta_beta)
-
-        def summary(e, t):
-            rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
-                   "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
-            sps = X / t
-            return {"ess_per_sample": e["ESS"] / X, "ess_per_s": e["ESS"] / t, "samples_per_s": sps,
-                    "Z": e["Z"], "Z error": e["Z error"], "E": e["jk_E"], "E error": e["jk_E error"],
-                    "Cv": e["jk_Cv"], "Cv error": e["jk_Cv error"],
-                    "time_to_1e-3_s": {k: X * (v / 1e-3) ** 2 / sps for k, v in rel.items()}}
-        sp, sl = summary(ep, tp), summary(ef, tf)
+        del res
+        sp, sl = rate_summary(ep, tp, X), rate_summary(ef, tf, X, train_s)
+        ratio = {k: (sp["time_to_1e-3_s"][k] / sl["time_to_1e-3_s"][k]
+                     if sp["time_to_1e-3_s"][k] and sl["time_to_1e-3_s"][k] else None) for k in ("Z", "E", "Cv")}
         agree = {k: abs(sl[k] - sp[k]) / math.hypot(sl[k + " error"], sp[k + " error"]) for k in ("Z", "E", "Cv")}
-        out["models"].append({"model_seed": seed, "plain": sp, "learned": sl, "train_s": t_train + t2,
+        out["models"].append({"model_seed": seed, "plain": sp, "learned": sl,
+                              "train_s": train_s,
+                              "train_parts_s": {"rho_samples_2e6": t_draw, "round1": t_train1,
+                                                "own_samples_1e6": t_own, "round2": t_train2},
                               "ess_per_s_ratio": sl["ess_per_s"] / sp["ess_per_s"],
-                              "wall_to_1e-3_ratio": max(sp["time_to_1e-3_s"].values()) / max(sl["time_to_1e-3_s"].values()),
+                              "proposal_overhead": sp["samples_per_s"] / sl["samples_per_s"] - 1.0,
+                              "wall_to_1e-3_ratio_incl_training": ratio,
                               "agreement_sigma": agree})
     out["median_ess_per_s_ratio"] = statistics.median(m["ess_per_s_ratio"] for m in out["models"])
     return out
@@ -567,13 +628,16 @@ def large_leg(args):
     from pibronic_gb300.flow import FlowProposal
     from pibronic_gb300.pimc import evaluate_device
     A, N, P, T = 12, 64, 256, 300.0
-    X = args.large_samples
+    X, Ct = args.large_samples, 400_000
     data = large_model_data(T)
     plan = data.plan
     assert plan.use_tc
     evaluate_device(plan, 1000, seed=9, offset=0)
-    plain, tp = _timed(torch, lambda: evaluate_device(plan, X, seed=1, offset=0, want_q=True))
+    # the flow's training samples (rho's own, with their q: 26 GB at 4e5 samples)
+    train_pl, t_draw = _timed(torch, lambda: evaluate_device(plan, Ct, seed=1001, offset=0, want_q=True))
+    plain, tp = _chunked(torch, lambda n, off: evaluate_device(plan, n, seed=1, offset=off), X, 2_000_000)
     ep = stats.device_estimates(plain["s_rho"], plain["s_g"], plain["s_gp"], plain["s_gm"], T, data.delta_beta)
+    del plain
     # the tcgen05 GEMM alone on one L2-sized chunk of this run's q
     lib = _native.load()
     n2p, a2p = ctypes.c_int32(), ctypes.c_int32()
@@ -586,7 +650,7 @@ def large_leg(args):
     sh = _native.stream_handle()
     _native.check(lib.pbr_tc_pack_potential(t_["vib_qq"].data_ptr(), t_["vib_l"].data_ptr(), t_["vib_e"].data_ptr(),
                                             32, N, A, _native.ptr(bp), sh), "pack")
-    qc = plain["q"][:Xc]
+    qc = train_pl["q"][:Xc]
     ts = []
     for i in range(4):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -607,16 +671,9 @@ def large_leg(args):
     _native.check(lib.pbr_tc_mma_rate(128, 256, 4096, _native.ptr(probe), ctypes.byref(rate), ctypes.byref(cyc), sh),
                   "mma rate")
 
-    def summary(e, t):
-        rel = {"Z": e["Z error"] / abs(e["Z"]), "E": e["jk_E error"] / abs(e["jk_E"]),
-               "Cv": e["jk_Cv error"] / abs(e["jk_Cv"])}
-        sps = X / t
-        return {"samples_per_s": sps, "ess_per_sample": e["ESS"] / X, "ess_per_s": e["ESS"] / t,
-                "Z": e["Z"], "Z error": e["Z error"], "E": e["jk_E"], "E error": e["jk_E error"],
-                "Cv": e["jk_Cv"], "Cv error": e["jk_Cv error"],
-                "time_to_1e-3_s": {k: X * (v / 1e-3) ** 2 / sps for k, v in rel.items()}}
-    out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K dense Q N(0,0.001) eV, dbeta=1e-4 beta, {X} samples",
-           "plain": summary(ep, tp),
+    out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K dense Q N(0,0.001) eV, dbeta=1e-4 beta, {X} samples per "
+                       f"estimate; flow over 2 ring slots per mode trained on {Ct} rho samples",
+           "plain": rate_summary(ep, tp, X),
            "tc_gemm": {"chunk_samples": Xc, "ms": 1e3 * t_tc, "issued_tflops": issued, "useful_tflops": useful,
                        "tf32_cublas_tflops_measured": peak, "frac_of_measured_tf32": issued / peak,
                        "tf32_mma_128x256x8_tflops_measured": rate.value,
@@ -625,20 +682,25 @@ def large_leg(args):
                        "note": "issued = 3 TF32 passes (hi/lo split) x padded K x padded pair columns"}}
     if not args.no_learned:
         fl = FlowProposal(data.prepared, plan, nsel=2, layers=8, hidden=128, seed=0)
-        y, _ = fl.prepare(plain["q"])
-        r = plain["s_g"] / plain["s_rho"]
-        del plain["q"]
+        y, _ = fl.prepare(train_pl["q"])
+        r = train_pl["s_g"] / train_pl["s_rho"]
+        del train_pl
         _warm_training(torch, FlowProposal, data.prepared, plan, 2, y, r)
         _, t_train = _timed(torch, lambda: fl.train(y, r, epochs=6, batch=16384, lr=1e-3))
         del y
         fl.sample_and_evaluate(1000, seed=5)
-        res, tf = _timed(torch, lambda: fl.sample_and_evaluate(X, seed=8))
+        res, tf = _chunked(torch, lambda n, off: fl.sample_and_evaluate(n, seed=8, offset=off), X, Ct)
         ef = stats.device_estimates(res["s_q"], res["s_g"], res["s_gp"], res["s_gm"], T, data.delta_beta)
-        sl = summary(ef, tf)
+        del res
+        train_s = t_draw + t_train
+        sl = rate_summary(ef, tf, X, train_s)
         sp = out["plain"]
         out["learned"] = sl
-        out["train_s"] = t_train
+        out["train_s"] = train_s
         out["ess_per_s_ratio"] = sl["ess_per_s"] / sp["ess_per_s"]
+        out["wall_to_1e-3_ratio_incl_training"] = {
+            k: (sp["time_to_1e-3_s"][k] / sl["time_to_1e-3_s"][k]
+                if sp["time_to_1e-3_s"][k] and sl["time_to_1e-3_s"][k] else None) for k in ("Z", "E", "Cv")}
         out["agreement_sigma"] = {k: abs(sl[k] - sp[k]) / math.hypot(sl[k + " error"], sp[k + " error"])
                                   for k in ("Z", "E", "Cv")}
     return out
@@ -660,6 +722,31 @@ def large_model_data(T=300.0):
     data.blocks = 1
     data.preprocess()
     return data
+
+
+def precision_leg(args):
+    """The precision configuration: the main workload's model (A=4, N=12, P=64) at T = 100, 300 and
+    500 K, args.precision_samples device-drawn samples each, evaluated by the FP32 production
+    kernel and by the FP64 build of the same kernel on identical q (pibronic_gb300.precision):
+    per-sample relative errors of rho, g, g(beta +- dbeta) and the FP32 - FP64 differences of Z, E
+    and Cv in units of their statistical errors."""
+    from pibronic_gb300 import constants, synthetic
+    from pibronic_gb300.plan import PreparedModels
+    from pibronic_gb300.precision import compare
+    m = synthetic.make_coupled_model(A_, N_, MODEL_SEED)
+    out = {"workload": f"A={A_} N={N_} P={P_}, {args.precision_samples} samples per temperature, "
+                       f"FP32 kernel vs FP64 build on identical q", "temperatures": []}
+    for T in (100.0, 300.0, 500.0):
+        b = constants.beta(T)
+        prep = PreparedModels(m, synthetic.diagonal_of(m), P_, beta=b, delta_beta=1e-4 * b)
+        res = compare(prep, args.precision_samples, seed=77, temperature=T)
+        out["temperatures"].append({"T": T, "per_sample": res["per_sample"], "estimates": res["estimates"],
+                                    "ess_per_sample": res["ess_per_sample"]})
+    out["max_per_sample_rel"] = max(v["max_rel"] for t in out["temperatures"]
+                                    for k, v in t["per_sample"].items() if k.startswith("s_"))
+    out["max_abs_delta_over_sigma"] = max(abs(v["delta_over_sigma"]) for t in out["temperatures"]
+                                          for v in t["estimates"].values())
+    return out
 
 
 def profile_large(args):
@@ -739,14 +826,16 @@ def main():
     ap.add_argument("--cpu-samples", type=int, default=400, help="samples per host process (CPU legs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variant", type=int, default=0, help="fused-kernel form: 0 auto, 1 chunks, 2 teams")
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--precision-samples", type=int, default=1_000_000)
     ap.add_argument("--no-learned", action="store_true")
-    ap.add_argument("--learned-samples", type=int, default=1_000_000)
+    ap.add_argument("--learned-samples", type=int, default=10_000_000)
     ap.add_argument("--learned-seeds", type=int, nargs="+", default=[404, 44, 4])
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-models", type=int, default=256)
     ap.add_argument("--batch-samples", type=int, default=100_000)
     ap.add_argument("--no-large", action="store_true")
-    ap.add_argument("--large-samples", type=int, default=400_000)
+    ap.add_argument("--large-samples", type=int, default=10_000_000)
     ap.add_argument("--profile-large", type=int, default=0,
                     help="profiling helper: evaluate this many samples of the large configuration twice, exit")
     ap.add_argument("--profile-learned", type=int, default=0,

@@ -209,20 +209,48 @@ class DeviceReducer:
 
     def launch(self, rho, g, gp, gm, delta_beta, temperature, stream=None):
         """Queue both passes on the stream (nothing is read back)."""
-        lib = _native.load()
-        sh = _native.stream_handle(stream)
-        p = _native.ptr
-        _native.check(lib.pbr_reduce_terms(p(rho), p(g), p(gp), p(gm), self.X, float(delta_beta),
-                                           p(self.scratch), p(self.moments), sh), "reduce_terms")
+        self.launch_terms(rho, g, gp, gm, delta_beta, stream)
         if gp is None:
             return 3
         # totals S_r, S_1, S_2 = n * mean, computed on the device without a host round trip
         self.totals.copy_(self.moments[[1, 3, 5]] * self.moments[0])
+        self.launch_jackknife(rho, g, gp, gm, delta_beta, temperature, stream)
+        return 5
+
+    def launch_terms(self, rho, g, gp, gm, delta_beta, stream=None):
+        """First pass: moments of r, s1, s2 over these samples into self.moments."""
+        lib = _native.load()
+        p = _native.ptr
+        _native.check(lib.pbr_reduce_terms(p(rho), p(g), p(gp), p(gm), self.X, float(delta_beta),
+                                           p(self.scratch), p(self.moments), _native.stream_handle(stream)),
+                      "reduce_terms")
+
+    def launch_jackknife(self, rho, g, gp, gm, delta_beta, temperature, stream=None):
+        """Second pass over these samples against the totals in self.totals (which may be the
+        totals of a larger sample set, e.g. all ranks' samples) into self.jk."""
+        lib = _native.load()
+        p = _native.ptr
         kT2 = boltzman * temperature ** 2
         _native.check(lib.pbr_reduce_jackknife(p(rho), p(g), p(gp), p(gm), self.X, float(delta_beta),
                                                float(kT2), p(self.totals), p(self.scratch),
-                                               p(self.jk), sh), "reduce_jackknife")
-        return 5
+                                               p(self.jk), _native.stream_handle(stream)), "reduce_jackknife")
+
+    def pooled(self, rho, g, gp, gm, delta_beta, temperature, group=None, stream=None):
+        """Both passes with the estimates and the jackknife taken over every rank's samples
+        (torch.distributed): see shard.pooled_moments.  Returns the estimates dict."""
+        from .shard import pooled_moments
+        torch = _native.require_cuda()
+
+        def pass1():
+            self.launch_terms(rho, g, gp, gm, delta_beta, stream)
+            return self.moments.cpu().numpy()
+
+        def pass2(totals):
+            self.totals.copy_(torch.as_tensor(totals, dtype=torch.float64))
+            self.launch_jackknife(rho, g, gp, gm, delta_beta, temperature, stream)
+            return self.jk.cpu().numpy()
+        m, j = pooled_moments(pass1, pass2, group)
+        return estimates_from_moments(m, j, temperature)
 
     def read(self, temperature):
         m = self.moments.cpu().numpy()

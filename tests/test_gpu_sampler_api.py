@@ -283,3 +283,19 @@ def test_errors_are_reported_not_faulted(tmp_path):
     rho1[vibronic_io.VMK.A] = 1
     with pytest.raises(AssertionError):
         PreparedModels(vib, rho1, 12, temperature=300.0)
+
+
+def test_pooled_reduction_on_one_process_equals_the_plain_one(tmp_path):
+    """DeviceReducer.pooled (the multi-rank jackknife of shard.pooled_moments) without a process
+    group runs the same two passes as DeviceReducer.launch."""
+    from pibronic_gb300 import stats
+    from pibronic_gb300.pimc import evaluate_device
+    FS, data = make_box(tmp_path, A=3, N=5, P=16, X=50000)
+    out = evaluate_device(data.plan, 50000, seed=3, offset=0)
+    args = (out["s_rho"], out["s_g"], out["s_gp"], out["s_gm"], data.delta_beta, data.temperature)
+    red = stats.DeviceReducer(50000)
+    pooled = red.pooled(*args)
+    plain = stats.device_estimates(out["s_rho"], out["s_g"], out["s_gp"], out["s_gm"], data.temperature,
+                                   data.delta_beta)
+    for k, v in plain.items():
+        assert v == pooled[k], k
