@@ -596,14 +596,15 @@ def learned_leg(args):
     return out
 
 
-def tf32_cublas_peak(torch):
-    """cuBLAS TF32 dense GEMM throughput measured in this run (8192^3, best of 5, CUDA events):
-    the denominator for the tcgen05 TF32 kernel (MEASURED_PEAKS.json holds the bf16 peak only)."""
+def cublas_peak(torch, dtype):
+    """cuBLAS dense GEMM throughput measured in this run (8192^3, best of 5, CUDA events), FP32
+    inputs with TF32 math or 16-bit inputs: the denominators for the tcgen05 kernels (the pool's
+    MEASURED_PEAKS.json holds a bf16 figure measured outside this run)."""
     old = torch.backends.cuda.matmul.allow_tf32
     torch.backends.cuda.matmul.allow_tf32 = True
     n = 8192
-    a = torch.randn(n, n, device="cuda")
-    b = torch.randn(n, n, device="cuda")
+    a = torch.randn(n, n, device="cuda").to(dtype)
+    b = torch.randn(n, n, device="cuda").to(dtype)
     c = a @ b
     best = float("inf")
     for _ in range(5):
@@ -662,24 +663,31 @@ def large_leg(args):
         if i:
             ts.append(e0.elapsed_time(e1) * 1e-3)
     t_tc = min(ts)
-    mp = int(lib.pbr_tc_potential_packed_floats(N, A)) // (2 * n2p)     # pair columns incl. padding
+    mp = a2p                                                             # pair columns incl. padding
     issued = 6.0 * Xc * P * mp * n2p / t_tc / 1e12
     useful = 2.0 * Xc * P * (A * (A + 1) // 2) * (N * (N + 1) // 2 + N + 1) / t_tc / 1e12
-    peak = tf32_cublas_peak(torch)
-    rate, cyc = ctypes.c_double(), ctypes.c_double()
+    peak16 = cublas_peak(torch, torch.float16)
     probe = torch.empty(2, dtype=torch.float64, device="cuda")
-    _native.check(lib.pbr_tc_mma_rate(128, 256, 4096, _native.ptr(probe), ctypes.byref(rate), ctypes.byref(cyc), sh),
-                  "mma rate")
+
+    def mma_rate(fmt, n_cols):
+        rate, cyc = ctypes.c_double(), ctypes.c_double()
+        _native.check(lib.pbr_tc_mma_rate(fmt, 128, n_cols, 1, 0, 4096, _native.ptr(probe), ctypes.byref(rate),
+                                          ctypes.byref(cyc), sh), "mma rate")
+        return rate.value, cyc.value
+    r256, c256 = mma_rate(1, 256)
+    rN, cN = mma_rate(1, mp)
 
     out = {"workload": f"A={A} N={N} P={P} T={T:.0f}K dense Q N(0,0.001) eV, dbeta=1e-4 beta, {X} samples per "
                        f"estimate; flow over 2 ring slots per mode trained on {Ct} rho samples",
            "plain": rate_summary(ep, tp, X),
            "tc_gemm": {"chunk_samples": Xc, "ms": 1e3 * t_tc, "issued_tflops": issued, "useful_tflops": useful,
-                       "tf32_cublas_tflops_measured": peak, "frac_of_measured_tf32": issued / peak,
-                       "tf32_mma_128x256x8_tflops_measured": rate.value,
-                       "cycles_per_mma_measured": cyc.value,
-                       "frac_of_measured_mma_rate": issued / rate.value,
-                       "note": "issued = 3 TF32 passes (hi/lo split) x padded K x padded pair columns"}}
+                       "fp16_cublas_tflops_measured": peak16, "frac_of_measured_fp16": issued / peak16,
+                       "f16_mma_128x256x16_tflops_measured": r256, "cycles_per_mma_n256": c256,
+                       f"f16_mma_128x{mp}x16_tflops_measured": rN, f"cycles_per_mma_n{mp}": cN,
+                       "frac_of_mma_rate_at_its_n": issued / rN,
+                       "note": "issued = 3 FP16 passes (hi/lo split) x padded K x padded pair columns; "
+                               "a kind::f16 MMA costs the same cycles for every N up to 128, so at "
+                               f"N = {mp} the tensor pipe's ceiling is the rate at that N"}}
     if not args.no_learned:
         fl = FlowProposal(data.prepared, plan, nsel=2, layers=8, hidden=128, seed=0)
         y, _ = fl.prepare(train_pl["q"])
@@ -788,6 +796,32 @@ def profile_learned(args):
     return 0
 
 
+def mma_rates(args):
+    """Profiling helper (no JSON line): the library's tcgen05 rate probe over operand type, M, N,
+    independent accumulators and the A operand's home, one row per shape (cycles per MMA of the
+    issuing thread and whole-GPU TF/s)."""
+    import ctypes
+    import torch
+    from pibronic_gb300 import _native
+    from pibronic_gb300.build import build
+    lib = _native.load(build())
+    probe = torch.empty(2, dtype=torch.float64, device="cuda")
+    sh = _native.stream_handle()
+    print("kind  M    N  accumulators  A_in_tmem  cycles_per_mma  TF/s")
+    for fmt, kind in ((2, "tf32"), (1, "f16")):
+        for M in (128, 64):
+            for N in (16, 32, 64, 80, 96, 128, 160, 256):
+                for nacc in (1, 2, 4):
+                    for at in ((0, 1) if (fmt == 2 and M == 128) else (0,)):
+                        if nacc * N + (16 if at else 0) > 512:
+                            continue
+                        r, c = ctypes.c_double(), ctypes.c_double()
+                        _native.check(lib.pbr_tc_mma_rate(fmt, M, N, nacc, at, 4096, _native.ptr(probe),
+                                                          ctypes.byref(r), ctypes.byref(c), sh), "mma rate")
+                        print(f"{kind:5s} {M:3d} {N:4d} {nacc:13d} {at:10d} {c.value:15.1f} {r.value:7.1f}")
+    return 0
+
+
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
     each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
@@ -841,7 +875,11 @@ def main():
     ap.add_argument("--profile-learned", type=int, default=0,
                     help="profiling helper: evaluate this many plain-rho samples of the learned "
                          "configuration's model twice, exit")
+    ap.add_argument("--mma-rates", action="store_true",
+                    help="profiling helper: sweep the tcgen05 rate probe, print a table, exit")
     args = ap.parse_args()
+    if args.mma_rates:
+        return mma_rates(args)
     if args.profile_large > 0:
         return profile_large(args)
     if args.profile_learned > 0:

@@ -401,13 +401,16 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
  * from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in pbr_tc_gemm.  Replaces
  * pimc.py:1145-1150 (V of diagonalize_coupling_matrix).
  */
-/* Tensor-pipe rate: one CTA per SM issues reps back-to-back tcgen05.mma kind::tf32 (M x N x 8,
- * M 64 or 128, 16 <= N <= 256) from one thread; *tflops is the whole-GPU rate, *cycles_per_mma the
- * issuing thread's cycles per instruction.  scratch: 16 bytes of the caller's device memory,
- * 8-byte aligned (the cycle count and the kernel's wait flag).  Synchronizes the stream to read the
- * result (a measurement, not a path entry point).  No counterpart in the reference. */
-int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch, double* tflops, double* cycles_per_mma,
-                    void* stream);
+/* Tensor-pipe rate: one CTA per SM issues reps back-to-back tcgen05.mma from one thread --
+ * fmt 2: kind::tf32, M x N x 8; fmt 1: kind::f16 with BF16 operands, M x N x 16 (M 64 or 128,
+ * 16 <= N <= 256) -- round-robin over nacc (1..4) independent TMEM accumulators, A from shared
+ * memory or (a_tmem = 1, TF32, M = 128) from TMEM; *tflops is the whole-GPU rate,
+ * *cycles_per_mma the issuing thread's cycles per instruction.  scratch: 16 bytes of the caller's
+ * device memory, 8-byte aligned (the cycle count and the kernel's wait flag).  Synchronizes the
+ * stream to read the result (a measurement, not a path entry point).  No counterpart in the
+ * reference. */
+int pbr_tc_mma_rate(int32_t fmt, int32_t M, int32_t N, int32_t nacc, int32_t a_tmem, int32_t reps, void* scratch,
+                    double* tflops, double* cycles_per_mma, void* stream);
 
 int pbr_tc_potential_dims(int32_t N, int32_t A, int32_t* n2p, int32_t* a2p);
 int64_t pbr_tc_potential_packed_floats(int32_t N, int32_t A);

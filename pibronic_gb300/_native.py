@@ -122,7 +122,7 @@ def _declare(lib):
         "pbr_tc_gemm": (C.c_int, [i32, vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential_dims": (C.c_int, [i32, i32, C.POINTER(i32), C.POINTER(i32)]),
         "pbr_tc_potential_packed_floats": (i64, [i32, i32]),
-        "pbr_tc_mma_rate": (C.c_int, [i32, i32, i32, vp, C.POINTER(f64), C.POINTER(f64), vp]),
+        "pbr_tc_mma_rate": (C.c_int, [i32, i32, i32, i32, i32, i32, vp, C.POINTER(f64), C.POINTER(f64), vp]),
         "pbr_tc_pack_potential": (C.c_int, [vp, vp, vp, i32, i32, i32, vp, vp]),
         "pbr_tc_potential": (C.c_int, [vp, i64, i32, i32, i32, vp, vp, vp, vp]),
         "pbr_sample_eval_tc_scratch": (i64, [C.POINTER(PbrModel), i64]),

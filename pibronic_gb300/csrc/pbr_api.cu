@@ -450,7 +450,7 @@ int run_tc(const pbr_model* model, const float* q_in, uint64_t seed, uint64_t of
     const int chk = q_in ? check_model(m, kQ32, q_in, out, PBR_MAX_A_WIDE)
                          : check_model(m, kSample, nullptr, out, PBR_MAX_A_WIDE);
     if (chk != PBR_OK) return chk;
-    if (m.precision != 32) return PBR_ERR_UNSUPPORTED;        // TF32 split: the FP32 form only
+    if (m.precision != 32) return PBR_ERR_UNSUPPORTED;        // FP16 split: the FP32 form only
     const bool wide = m.A > PBR_MAX_A;
     if (reinterpret_cast<uintptr_t>(scratch) % kScratchAlign) return PBR_ERR_ARG;
     const int64_t per = tc_sample_bytes(m);
@@ -486,7 +486,7 @@ int run_tc(const pbr_model* model, const float* q_in, uint64_t seed, uint64_t of
             if (rc != PBR_OK) return rc;
             qc = qs;
         }
-        rc = tc_quadratic_launch(qc, n, m.N, m.P, A2P, bpack, vq, out->status, st);
+        rc = tc_quadratic_launch(qc, n, m.N, m.P, m.A, bpack, vq, out->status, st);
         if (rc != PBR_OK) return rc;
         pbr_outputs oc = *out;
         oc.s_rho = out->s_rho + c0;

@@ -9,6 +9,8 @@
 // its TMEM.
 #include <cstdint>
 
+#include <cuda_fp16.h>
+
 #include "pbr_common.cuh"
 
 namespace {
@@ -222,14 +224,24 @@ extern "C" int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, 
 // slots s = [q_0 .. q_{N-1}, 0 .. (to NA = N rounded up to 4), 1, 0, 0, 0].  Quads (d, e0) for
 // d < N and e0 = 0, 4, .. <= d cover the quadratic pairs e <= d (Bm = the symmetrised 1/2 Q
 // couplings, zero for e > d), quads (NA, j0) the linear terms (Bm = L_e for e < N), quad (NA, NA)
-// the energies (Bm = E at its first column); quads (NA + 1, NA) = 0 pad K to a multiple of 32.
+// the energies (Bm = E at its first column); quads (NA + 1, NA) = 0 pad K to a multiple of 64.
 //
-// TF32 with a hi/lo split of both operands: three MMAs per K step (hi*hi + hi*lo + lo*hi), FP32
-// accumulation in TMEM, about 21 bits kept per product (the accuracy of the FP32 FMA form).
+// FP16 with a hi/lo split of both operands: three tcgen05.mma kind::f16 per K step of 16
+// (hi*hi + hi*lo + lo*hi), FP32 accumulation in TMEM, about 22 bits kept per product (the
+// accuracy of the FP32 FMA form).  A kind::f16 MMA of M = 128, K = 16 costs 74 cycles for any
+// N <= 128 on GB300, a kind::tf32 one of K = 8 costs 142 (measured by pbr_tc_mma_rate), so the
+// FP16 split does the same K in 26 % of the tensor-pipe time of a TF32 split.  FP16's range is
+// kept by exact power-of-two scaling: every bead row's products are scaled by 2^s_row so that
+// the largest is below 2^14 (its largest coordinate squared decides s_row), the couplings by one
+// global 2^s_B so that the largest is below 2^14; hi and lo then stay normal FP16 numbers except
+// for entries 2^-25 or less of the largest, whose absolute error is below 2^-39 of it.  The
+// first padding column of the couplings (pair A2, always < A2P for A <= 16) holds 1 at the
+// energies' K column, so the accumulator's column A2 returns 2^s_row for its row, and the
+// epilogue divides the row by 2^s_row * 2^s_B exactly.
 // Warp-specialised persistent CTA, one 128-row tile at a time:
-//   warps 0-7   generate the A operand stage by stage (two threads per row, four quads each: one
-//               broadcast load of q_d, one 128-bit load of q_e0..e0+3, hi / lo by masking to TF32)
-//               from the tile's bead coordinates, which they prefetch one tile ahead (cp.async);
+//   warps 0-7   generate the A operand stage by stage (two threads per row, eight quads each: the
+//               row's q_d and q_e0..e0+3 from shared memory, hi / lo as FP16 pairs) from the
+//               tile's bead coordinates, which they prefetch one tile ahead (cp.async);
 //   warp 8      issues the tcgen05.mma of each stage once its A and B operands are in place;
 //   warp 9      streams the B stages (packed on the device in the shared-memory core layout) with
 //               cp.async.bulk; when all stages fit they are loaded once and stay resident;
@@ -244,9 +256,11 @@ namespace {
 constexpr int kGenThreads = 256;                      // warps 0-7
 constexpr int kEpiThreads = 128;                      // warps 10-13
 constexpr int kPotThreads = kGenThreads + 64 + kEpiThreads;   // + MMA warp, B-loader warp, epilogue
-constexpr int kQStageK = 32;                          // TF32 elements of K per stage (128 B)
+constexpr int kQStageK = 64;                          // FP16 elements of K per stage (128 B per row)
 constexpr int kQuadsPerStage = kQStageK / 4;
-constexpr int kAStageCols = 2 * kQStageK;             // TMEM columns of one A stage (hi, lo)
+constexpr int kAPartCols = kQStageK / 2;              // TMEM columns of one A part (two FP16 per column)
+constexpr int kAStageCols = 2 * kAPartCols;           // TMEM columns of one A stage (hi, lo)
+constexpr int kKMma = 16;                             // K of one kind::f16 MMA
 
 // slot of the constant 1, and the number of slots per bead row (q, zeros, 1, 0, 0, 0)
 __host__ __device__ inline int q_one(int N) { return (N + 3) / 4 * 4; }
@@ -268,6 +282,15 @@ __host__ __device__ inline void quad_of(int qi, int N, int& d, int& e0) {
     if (qi < nl) { d = na; e0 = 4 * qi; return; }       // linear
     if (qi == nl) { d = na; e0 = na; return; }          // energies
     d = na + 1; e0 = na;                                // padding: 0 * [1, 0, 0, 0]
+}
+
+// K column of the energies (the first column of quad (NA, NA)), where a = 1 for every row
+__host__ __device__ inline int energy_column(int N) { return 4 * (quad_count(N) - 1); }
+
+// power of two 2^(14 - e) with x < 2^e (x positive, normal, finite): x * result < 2^14
+__device__ __forceinline__ float fp16_range_scale(float x) {
+    const int e = static_cast<int>((__float_as_uint(x) >> 23) & 0xFFu) - 126;
+    return __uint_as_float(static_cast<uint32_t>(127 + 14 - e) << 23);
 }
 
 // shared memory: B stages, two tiles of bead coordinates (mode-major: slot j of row r at
@@ -322,20 +345,28 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float tf32_trunc(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// one FP32 accumulator column of this warp's 32 TMEM lanes
+__device__ __forceinline__ float tmem_ld1(uint32_t taddr) {
+    uint32_t r;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];" : "=r"(r) : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    return __uint_as_float(r);
+}
 
 // 16 consecutive 32-bit TMEM columns of this warp's 32 lanes
-__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t (&v)[16]) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
         "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
-        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
-          "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
-          "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
-          "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
-          "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
-          "r"(__float_as_uint(v[15]))
+        ::"r"(taddr), "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+          "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15])
         : "memory");
+}
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+    uint32_t u[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) u[i] = __float_as_uint(v[i]);
+    tmem_st16(taddr, u);
 }
 
 // D (TMEM) += A (TMEM, K-major: lane = row, 32-bit column = k) x B (shared memory descriptor)
@@ -347,10 +378,29 @@ __device__ __forceinline__ void mma_tf32_ts(uint32_t tmem_d, uint32_t tmem_a, ui
         ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-__device__ __forceinline__ float tf32_rna(float x) {
+// D (TMEM) += A (TMEM, K-major: lane = row, 32-bit column = the FP16 pair k, k + 1 with k in the
+// low half) x B (shared memory descriptor, FP16); both operands FP16
+__device__ __forceinline__ void mma_f16_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n"
+        ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+// FP16 pair (x0, x1), x0 in the low half
+__device__ __forceinline__ uint32_t pack_f16x2(float x0, float x1) {
     uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(x1), "f"(x0));
+    return r;
+}
+
+// hi = FP16(x) and lo = FP16(x - hi) for two values, packed as FP16 pairs
+__device__ __forceinline__ void split_f16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    hi = pack_f16x2(x0, x1);
+    const __half2 h = *reinterpret_cast<const __half2*>(&hi);
+    const float2 hf = __half22float2(h);
+    lo = pack_f16x2(x0 - hf.x, x1 - hf.y);
 }
 
 // bounded wait that gives up early once another role has recorded an error
@@ -370,8 +420,9 @@ __device__ __forceinline__ bool mbar_wait_or_err(uint64_t* bar, uint32_t parity,
 }
 
 __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
-        const float* __restrict__ q, int64_t X, int N, int P, int nst, int A2P, int nbuf,
-        const unsigned char* __restrict__ bpack, float* __restrict__ vq, int ncols, int32_t* status) {
+        const float* __restrict__ q, int64_t X, int N, int P, int nst, int A2, int A2P, int nbuf,
+        const unsigned char* __restrict__ bpack, const float* __restrict__ b_scale, float* __restrict__ vq,
+        int ncols, int32_t* status) {
     extern __shared__ __align__(1024) unsigned char tsm[];
     const PotSmem L(N, A2P, nst, nbuf);
     const int NB = L.nb;
@@ -471,28 +522,30 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                 ok = mbar_wait_or_err(sq_ready, tl & 1, err);
             }
             const float* myq = sq + (tl & 1) * kBM * NSL + row_l;
+            // the row's scale 2^s_row: its largest product (max(1, max_j q_j^2)) times 2^s_row
+            // stays below 2^14; NaN or Inf coordinates leave the products non-finite
+            float qmax = 1.f;
+            for (int j = 0; j < N; ++j) qmax = fmaxf(qmax, fabsf(myq[j * kBM]));
+            const float srow = fp16_range_scale(fminf(qmax * qmax, 3.0e38f));
             for (int st = 0; st < nst; ++st, ++it) {
                 const int b = it % NB, use = it / NB;
                 if (ok && use > 0) ok = mbar_wait_or_err(empty + b, (use - 1) & 1, err);
                 if (!ok) continue;
-                // this thread's row, K columns half * 16 .. half * 16 + 15 of the stage
-                float hi[16], lo[16];
+                // this thread's row, K columns half * 32 .. half * 32 + 31 of the stage
+                uint32_t hi[16], lo[16];
 #pragma unroll
                 for (int u = 0; u < kQuadsPerStage / 2; ++u) {
                     const uint32_t de = squad[st * kQuadsPerStage + half * (kQuadsPerStage / 2) + u];
                     const int d = static_cast<int>(de & 0xFFFFu), e0 = static_cast<int>(de >> 16);
-                    const float qd = myq[d * kBM];
-#pragma unroll
-                    for (int v = 0; v < 4; ++v) {
-                        const float x = qd * myq[(e0 + v) * kBM];
-                        const float h = tf32_trunc(x);
-                        hi[4 * u + v] = h;
-                        lo[4 * u + v] = x - h;           // the tensor core reads its TF32 bits
-                    }
+                    const float qd = myq[d * kBM] * srow;
+                    const float x0 = qd * myq[e0 * kBM], x1 = qd * myq[(e0 + 1) * kBM];
+                    const float x2 = qd * myq[(e0 + 2) * kBM], x3 = qd * myq[(e0 + 3) * kBM];
+                    split_f16x2(x0, x1, hi[2 * u], lo[2 * u]);
+                    split_f16x2(x2, x3, hi[2 * u + 1], lo[2 * u + 1]);
                 }
                 const uint32_t col = static_cast<uint32_t>(2 * A2P + b * kAStageCols + half * 16);
                 tmem_st16(tmem + lane_base + col, hi);
-                tmem_st16(tmem + lane_base + col + kQStageK, lo);
+                tmem_st16(tmem + lane_base + col + kAPartCols, lo);
                 asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
                 asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
                 mbar_arrive(full_a + b);
@@ -503,6 +556,7 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     } else if (warp >= 10) {
         // ======================= epilogue warpgroup: TMEM -> V =================================
         const int lg = warp & 3;                                  // TMEM lanes 32 lg .. 32 lg + 31
+        const float sb_inv = 1.0f / *b_scale;                     // 2^-s_B
         bool ok = true;
         for (int tl = 0; tl < my_tiles; ++tl) {
             ok = __all_sync(0xffffffffu, ok && !*err);
@@ -514,14 +568,18 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
             asm volatile("tcgen05.fence::after_thread_sync;");
             const int64_t r0 = (static_cast<int64_t>(blockIdx.x) + static_cast<int64_t>(tl) * gridDim.x) * kBM;
             const int64_t row = r0 + lg * 32 + lane;
+            const uint32_t tbase = tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(acc * A2P);
+            // column A2 = 2^s_row exactly: V = D / (2^s_row 2^s_B), exact powers of two
+            const float inv = sb_inv / tmem_ld1(tbase + static_cast<uint32_t>(A2));
             for (int c0 = 0; c0 < A2P; c0 += 16) {
                 float v[16];
-                tmem_ld16(tmem + (static_cast<uint32_t>(lg * 32) << 16) + static_cast<uint32_t>(acc * A2P + c0), v);
+                tmem_ld16(tbase + static_cast<uint32_t>(c0), v);
                 if (row < rows) {
                     float* dst = vq + row * A2P + c0;
 #pragma unroll
                     for (int i = 0; i < 16; i += 4)
-                        *reinterpret_cast<float4*>(dst + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                        *reinterpret_cast<float4*>(dst + i) =
+                            make_float4(v[i] * inv, v[i + 1] * inv, v[i + 2] * inv, v[i + 3] * inv);
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;");
@@ -530,7 +588,7 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
     } else if (warp == 8) {
         // ======================= MMA issuer (one thread) =======================================
         if (lane == 0) {
-            const uint32_t idesc = instr_desc(2, kBM, A2P);
+            const uint32_t idesc = instr_desc(0, kBM, A2P);        // FP16 x FP16 -> FP32
             constexpr uint32_t LBO = 128, SBO = (kStageBytesK / 16) * 128;
             uint64_t* last = nullptr;                 // barrier and parity of the latest commit
             uint32_t lastp = 0;
@@ -550,17 +608,18 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
                     }
                     asm volatile("tcgen05.fence::after_thread_sync;");
                     const uint32_t ahi = tmem + static_cast<uint32_t>(2 * A2P + b * kAStageCols);
-                    const uint32_t alo = ahi + kQStageK;
+                    const uint32_t alo = ahi + kAPartCols;
                     const unsigned char* bhi = sb + (resident ? st : b) * 2 * BSTAGE;
                     const unsigned char* blo = bhi + BSTAGE;
 #pragma unroll
-                    for (int kk = 0; kk < kQStageK; kk += 8) {
-                        const uint32_t off = static_cast<uint32_t>(kk * 4 / 16) * 128;
+                    for (int kk = 0; kk < kQStageK; kk += kKMma) {
+                        const uint32_t off = static_cast<uint32_t>(kk * 2 / 16) * 128;   // cores along K
                         const uint64_t dbh = smem_desc(smem_u32(bhi) + off, LBO, SBO);
                         const uint64_t dbl = smem_desc(smem_u32(blo) + off, LBO, SBO);
-                        mma_tf32_ts(dtm, ahi + kk, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
-                        mma_tf32_ts(dtm, ahi + kk, dbl, idesc, 1u);
-                        mma_tf32_ts(dtm, alo + kk, dbh, idesc, 1u);
+                        const uint32_t acol = static_cast<uint32_t>(kk / 2);            // two FP16 per column
+                        mma_f16_ts(dtm, ahi + acol, dbh, idesc, (st > 0 || kk > 0) ? 1u : 0u);
+                        mma_f16_ts(dtm, ahi + acol, dbl, idesc, 1u);
+                        mma_f16_ts(dtm, alo + acol, dbh, idesc, 1u);
                     }
                     mma_commit(empty + b);
                     last = empty + b;
@@ -609,13 +668,40 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
-// Qp [N2][A2], L [N][A2], E [A2] (FP32 or FP64; L and E nullable = zero) -> TF32 hi / lo in the
-// stage-major shared-memory core layout: stage s = [hi: A2P rows][lo: A2P rows], each row's 32
-// K columns as 8 cores of 4, core (row r, column c) at ((r / 8) * 8 + c) * 8 + r % 8 (16 B units).
+// 2^s_B for the couplings: the largest |entry| of Qp [N2][A2], L [N][A2], E [A2] (L, E nullable)
+// times 2^s_B stays below 2^14 (1 when every entry is zero).  One block; written to *scale.
+template <typename T>
+__global__ void tc_pack_scale_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en,
+                                     int N, int A2, float* __restrict__ scale) {
+    __shared__ float red[32];
+    const int64_t nq = static_cast<int64_t>(N) * (N + 1) / 2 * A2, nl = lin ? static_cast<int64_t>(N) * A2 : 0,
+                  ne = en ? A2 : 0;
+    float m = 0.f;
+    for (int64_t i = threadIdx.x; i < nq + nl + ne; i += blockDim.x) {
+        const T x = i < nq ? qq[i] : (i < nq + nl ? lin[i - nq] : en[i - nq - nl]);
+        m = fmaxf(m, fabsf(static_cast<float>(x)));
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+        m = fminf(m, 3.0e38f);
+        *scale = m > 0.f ? fp16_range_scale(fmaxf(m, 1.0e-30f)) : 1.f;
+    }
+}
+
+// Qp [N2][A2], L [N][A2], E [A2] (FP32 or FP64; L and E nullable = zero), times 2^s_B -> FP16
+// hi / lo in the stage-major shared-memory core layout: stage s = [hi: A2P rows][lo: A2P rows],
+// each row's 64 K columns as 8 cores of 8, core (row r, column c) at ((r / 8) * 8 + c) * 8 + r % 8
+// (16 B units), column k of the core in half k % 8.  Row A2 holds 1 at the energies' K column.
 template <typename T>
 __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en, int N,
-                               int A2, int nst, int A2P, float* __restrict__ out) {
+                               int A2, int nst, int A2P, const float* __restrict__ scale, __half* __restrict__ out) {
     const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;      // (stage, row, k in stage)
+    const float sB = *scale;
+    const int kone = energy_column(N);
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const int st = static_cast<int>(i / (static_cast<int64_t>(A2P) * kQStageK));
@@ -635,13 +721,16 @@ __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ l
             } else if (d == na && e0 == na) {
                 if (u == 0 && en) x = static_cast<float>(en[pr]);
             }
+            x *= sB;
+        } else if (pr == A2 && st * kQStageK + kk == kone) {
+            x = 1.f;
         }
-        const float h = tf32_rna(x);
-        const int c = kk / 4;
+        const __half h = __float2half_rn(x);
+        const int c = kk / 8;
         const int64_t base = static_cast<int64_t>(st) * 2 * A2P * kQStageK;
-        const int64_t slot = (static_cast<int64_t>((pr >> 3) * (kStageBytesK / 16) + c) * 8 + (pr & 7)) * 4 + u;
+        const int64_t slot = (static_cast<int64_t>((pr >> 3) * (kStageBytesK / 16) + c) * 8 + (pr & 7)) * 8 + kk % 8;
         out[base + slot] = h;
-        out[base + static_cast<int64_t>(A2P) * kQStageK + slot] = tf32_rna(x - h);
+        out[base + static_cast<int64_t>(A2P) * kQStageK + slot] = __float2half_rn(x - __half2float(h));
     }
 }
 
@@ -659,12 +748,16 @@ namespace pbr {
 
 int tc_quadratic_cols(int A) { return (A * (A + 1) / 2 + 15) / 16 * 16; }
 int tc_quadratic_kdim(int N) { return (quad_count(N) + kQuadsPerStage - 1) / kQuadsPerStage * kQStageK; }
-int64_t tc_packed_floats(int N, int A) { return static_cast<int64_t>(2) * tc_quadratic_cols(A) * tc_quadratic_kdim(N); }
+// FP16 hi and lo of A2P x K couplings (one 32-bit word per two), then 4 words: the scale 2^s_B
+int64_t tc_packed_floats(int N, int A) {
+    return static_cast<int64_t>(tc_quadratic_cols(A)) * tc_quadratic_kdim(N) + 4;
+}
 
-int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const void* bpack, float* vq,
+int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A, const void* bpack, float* vq,
                         int32_t* status, cudaStream_t stream) {
-    if (!q || !bpack || !vq || X < 0 || N < 1 || N > 64 || P < 1) return PBR_ERR_ARG;
-    if (A2P < 16 || A2P > 144 || A2P % 16 != 0) return PBR_ERR_ARG;
+    if (!q || !bpack || !vq || X < 0 || N < 1 || N > 64 || P < 1 || A < 1 || A > 16) return PBR_ERR_ARG;
+    const int A2 = A * (A + 1) / 2, A2P = tc_quadratic_cols(A);
+    if (A2P > 144) return PBR_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(bpack) | reinterpret_cast<uintptr_t>(vq)) & 15) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const int nst = tc_quadratic_kdim(N) / kQStageK;
@@ -686,28 +779,39 @@ int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A2P, const 
     // one CTA per SM: at least half the shared memory each, so two CTAs never share an SM's TMEM
     const int smem = L.total > 116 * 1024 ? L.total : 116 * 1024;
     const int grid = static_cast<int>(tiles < sms ? tiles : sms);
-    tc_potential_kernel<<<grid, kPotThreads, smem, stream>>>(q, X, N, P, nst, A2P, nb,
-                                                                 static_cast<const unsigned char*>(bpack), vq,
-                                                                 ncols, status);
+    const auto* bp = static_cast<const unsigned char*>(bpack);
+    const float* scale = reinterpret_cast<const float*>(bp + static_cast<int64_t>(A2P) * tc_quadratic_kdim(N) * 4);
+    tc_potential_kernel<<<grid, kPotThreads, smem, stream>>>(q, X, N, P, nst, A2, A2P, nb, bp, scale, vq, ncols,
+                                                                 status);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 
 int tc_pack_launch(const void* qq, const void* lin, const void* en, int precision, int N, int A, void* bpack,
                    cudaStream_t stream) {
     if (!qq || !bpack || N < 1 || N > 64 || A < 1 || A > 16) return PBR_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(bpack) & 15) return PBR_ERR_ARG;
     const int A2 = A * (A + 1) / 2;
     const int nst = tc_quadratic_kdim(N) / kQStageK, A2P = tc_quadratic_cols(A);
     const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;
     const int grid = static_cast<int>((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
-    float* out = static_cast<float*>(bpack);
-    if (precision == 32)
+    auto* out = static_cast<__half*>(bpack);
+    // the scale word after the 2 x A2P x K FP16 values (A2P x K x 4 bytes)
+    float* scale = reinterpret_cast<float*>(static_cast<unsigned char*>(bpack) + static_cast<int64_t>(A2P) * nst *
+                                            kQStageK * 4);
+    if (precision == 32) {
+        tc_pack_scale_kernel<float><<<1, 1024, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
+                                                            static_cast<const float*>(en), N, A2, scale);
         tc_pack_kernel<float><<<grid, 256, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
-                                                        static_cast<const float*>(en), N, A2, nst, A2P, out);
-    else if (precision == 64)
+                                                        static_cast<const float*>(en), N, A2, nst, A2P, scale, out);
+    } else if (precision == 64) {
+        tc_pack_scale_kernel<double><<<1, 1024, 0, stream>>>(static_cast<const double*>(qq),
+                                                             static_cast<const double*>(lin),
+                                                             static_cast<const double*>(en), N, A2, scale);
         tc_pack_kernel<double><<<grid, 256, 0, stream>>>(static_cast<const double*>(qq), static_cast<const double*>(lin),
-                                                         static_cast<const double*>(en), N, A2, nst, A2P, out);
-    else
+                                                         static_cast<const double*>(en), N, A2, nst, A2P, scale, out);
+    } else {
         return PBR_ERR_ARG;
+    }
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
 }
 
@@ -734,30 +838,31 @@ int pbr_tc_pack_potential(const void* vib_qq, const void* vib_l, const void* vib
 
 int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A, const void* b_packed, float* vq,
                      int32_t* status, void* stream) {
-    if (A < 1 || A > 16) return PBR_ERR_ARG;
-    return pbr::tc_quadratic_launch(q, X, N, P, pbr::tc_quadratic_cols(A), b_packed, vq, status,
-                                    static_cast<cudaStream_t>(stream));
+    return pbr::tc_quadratic_launch(q, X, N, P, A, b_packed, vq, status, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------------------
-// Tensor-pipe rate probe: each CTA (one per SM) issues `reps` back-to-back tcgen05.mma kind::tf32
-// (M x N x 8, operands zeros in shared memory, one TMEM accumulator) from one thread, commits once
-// and waits (bounded).  Reports the issuing thread's cycles per MMA and the whole-GPU TF/s; the
-// denominator the potential GEMM is held against.
+// Tensor-pipe rate probe: each CTA (one per SM) issues `reps` back-to-back tcgen05.mma (kind::tf32,
+// M x N x 8, or kind::f16 with BF16 operands, M x N x 16; operands zeros in shared memory, or the
+// TF32 A operand in TMEM) from one thread, round-robin over nacc independent TMEM accumulators,
+// commits once and waits (bounded).  Reports the issuing thread's cycles per MMA and the
+// whole-GPU TF/s: the denominator the potential GEMM is held against, and the evidence for what
+// an instruction costs (its shape, its operand type, its accumulator dependencies).
 // ---------------------------------------------------------------------------------------------
 namespace {
 
-__global__ void tc_rate_kernel(int M, int N, int reps, int32_t* flag, long long* cycles) {
+__global__ void tc_rate_kernel(int fmt, int M, int N, int nacc, int a_tmem, int reps, int32_t* flag,
+                               long long* cycles) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char* sa = sm;                 // 128 rows x 32 B (K = 8 tf32)
+    unsigned char* sa = sm;                 // 128 rows x 32 B (K = 8 tf32 or 16 bf16)
     unsigned char* sb = sm + 128 * 32;      // 256 rows x 32 B
     uint64_t* bar = reinterpret_cast<uint64_t*>(sm + 128 * 32 + 256 * 32);
     uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
     for (int i = threadIdx.x; i < (128 + 256) * 32 / 4; i += blockDim.x) reinterpret_cast<float*>(sm)[i] = 0.f;
     int ncols = 32;
-    while (ncols < N) ncols <<= 1;
+    while (ncols < nacc * N + (a_tmem ? 16 : 0)) ncols <<= 1;
     if (threadIdx.x < 32) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
                      "r"(ncols));
@@ -770,11 +875,32 @@ __global__ void tc_rate_kernel(int M, int N, int reps, int32_t* flag, long long*
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *slot;
+    const uint32_t ta = tmem + static_cast<uint32_t>(nacc * N);      // A operand: 16 columns (TMEM form)
+    if (a_tmem) {
+        // zero this warp's lanes of the A columns (warps 0-3 cover the 128 lanes)
+        float z[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) z[i] = 0.f;
+        const uint32_t lanes = static_cast<uint32_t>((threadIdx.x >> 5) * 32) << 16;
+        tmem_st16(ta + lanes, z);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
     if (threadIdx.x == 0) {
-        const uint32_t idesc = instr_desc(2, M, N);
+        const uint32_t idesc = instr_desc(fmt, M, N);
         const uint64_t da = smem_desc(smem_u32(sa), 128, 256), db = smem_desc(smem_u32(sb), 128, 256);
         const long long t0 = clock64();
-        for (int i = 0; i < reps; ++i) mma_issue<2>(tmem, da, db, idesc, i > 0 ? 1u : 0u);
+        int acc = 0;
+        for (int i = 0; i < reps; ++i) {
+            const uint32_t d = tmem + static_cast<uint32_t>(acc * N);
+            const uint32_t accumulate = i >= nacc ? 1u : 0u;
+            if (fmt == 1) mma_issue<1>(d, da, db, idesc, accumulate);
+            else if (a_tmem) mma_tf32_ts(d, ta, db, idesc, accumulate);
+            else mma_issue<2>(d, da, db, idesc, accumulate);
+            if (++acc == nacc) acc = 0;
+        }
         mma_commit(bar);
         const bool done = mbar_wait(bar, 0);
         const long long t1 = clock64();
@@ -789,10 +915,11 @@ __global__ void tc_rate_kernel(int M, int N, int reps, int32_t* flag, long long*
 
 }  // namespace
 
-extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch, double* tflops,
-                               double* cycles_per_mma, void* stream) {
-    if ((M != 64 && M != 128) || N < 16 || N > 256 || N % 16 != 0 || reps < 1 || reps > (1 << 20) || !tflops ||
-        !cycles_per_mma || !scratch || (reinterpret_cast<uintptr_t>(scratch) & 7) != 0)
+extern "C" int pbr_tc_mma_rate(int32_t fmt, int32_t M, int32_t N, int32_t nacc, int32_t a_tmem, int32_t reps,
+                               void* scratch, double* tflops, double* cycles_per_mma, void* stream) {
+    if ((fmt != 1 && fmt != 2) || (M != 64 && M != 128) || N < 16 || N > 256 || N % 16 != 0 || nacc < 1 ||
+        nacc > 4 || nacc * N + (a_tmem ? 16 : 0) > 512 || (a_tmem && (fmt != 2 || M != 128)) || reps < 1 ||
+        reps > (1 << 20) || !tflops || !cycles_per_mma || !scratch || (reinterpret_cast<uintptr_t>(scratch) & 7) != 0)
         return PBR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int dev = 0, sms = 0;
@@ -809,9 +936,9 @@ extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = PBR_ERR_CUDA;
     if (rc == PBR_OK && cudaMemsetAsync(scratch, 0, 16, st) != cudaSuccess) rc = PBR_ERR_CUDA;
     if (rc == PBR_OK) {
-        tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, 64, dflag, dcyc);        // warm-up
+        tc_rate_kernel<<<sms, 128, kSmem, st>>>(fmt, M, N, nacc, a_tmem, 64, dflag, dcyc);        // warm-up
         cudaEventRecord(e0, st);
-        tc_rate_kernel<<<sms, 128, kSmem, st>>>(M, N, reps, dflag, dcyc);
+        tc_rate_kernel<<<sms, 128, kSmem, st>>>(fmt, M, N, nacc, a_tmem, reps, dflag, dcyc);
         cudaEventRecord(e1, st);
         if (cudaGetLastError() != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) rc = PBR_ERR_CUDA;
     }
@@ -824,7 +951,8 @@ extern "C" int pbr_tc_mma_rate(int32_t M, int32_t N, int32_t reps, void* scratch
                          cudaStreamSynchronize(st) != cudaSuccess))
         rc = PBR_ERR_CUDA;
     if (rc == PBR_OK && flag) rc = PBR_ERR_CUDA;      // a wait in the kernel gave up
-    *tflops = (rc == PBR_OK && ms > 0.f) ? 2.0 * M * N * 8.0 * reps * sms / (ms * 1e-3) / 1e12 : 0.0;
+    const double kdim = fmt == 1 ? 16.0 : 8.0;
+    *tflops = (rc == PBR_OK && ms > 0.f) ? 2.0 * M * N * kdim * reps * sms / (ms * 1e-3) / 1e12 : 0.0;
     *cycles_per_mma = rc == PBR_OK ? static_cast<double>(cyc) / reps : 0.0;
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);

@@ -3,8 +3,9 @@ couplings) against an FP64 numpy contraction, and the tensor-core block evaluati
 (pbr_sample_eval_tc) against the oracle, the row-team form on the same samples, and itself under
 different chunkings.
 
-Tolerances: the GEMM keeps about 21 bits per product (TF32 hi/lo split, three MMAs) and
-accumulates in FP32, so |V - ref| <= 1e-5 * sum_k |a_k| |B_k| per entry; the block
+Tolerances: the GEMM keeps about 22 bits per product (FP16 hi/lo split of both operands after
+exact power-of-two scaling, three MMAs) and accumulates in FP32, so
+|V - ref| <= 1e-5 * sum_k |a_k| |B_k| per entry; the block
 evaluation is held to the FP32 production tolerance (rtol 2e-4 on rho, g, g(beta +- db))."""
 import numpy as np
 import pytest
@@ -34,7 +35,7 @@ def _quads(N):
     na = (N + 3) // 4 * 4
     qs = [(d, e0) for d in range(N) for e0 in range(0, d + 1, 4)]
     qs += [(na, j0) for j0 in range(0, N, 4)] + [(na, na)]
-    while len(qs) % 8:
+    while len(qs) % 16:
         qs.append((na + 1, na))
     return qs, na
 
@@ -61,19 +62,26 @@ def _expected_operands(N, A2, qq, lin, en, q_rows):
 
 
 def _unpack(bp, mp, n2p):
-    """b_packed (stages of 32 K columns, hi then lo, mp rows each, core layout) -> hi, lo [mp][n2p]."""
-    nst = n2p // 32
+    """b_packed (stages of 64 K columns, FP16 hi then lo, mp rows each, in the core layout; then
+    the FP32 scale 2^s_B) -> hi, lo [mp][n2p] (FP64) and the scale."""
+    words = bp.cpu().numpy()
+    h = words[:mp * n2p].view(np.float16).astype(np.float64)
+    nst = n2p // 64
     hi, lo = np.zeros((mp, n2p)), np.zeros((mp, n2p))
     r = np.arange(mp)[:, None]
-    c = np.arange(8)[None, :]
+    k = np.arange(64)[None, :]
+    idx = (((r // 8) * 8 + k // 8) * 8 + r % 8) * 8 + k % 8
     for st in range(nst):
-        base = st * 2 * mp * 32
+        base = st * 2 * mp * 64
         for part, dst in ((0, hi), (1, lo)):
-            blk = bp[base + part * mp * 32: base + (part + 1) * mp * 32]
-            for u in range(4):
-                idx = (((r // 8) * 8 + c) * 8 + r % 8) * 4 + u
-                dst[:, st * 32 + c[0] * 4 + u] = blk[idx]
-    return hi, lo
+            blk = h[base + part * mp * 64: base + (part + 1) * mp * 64]
+            dst[:, st * 64: (st + 1) * 64] = blk[idx]
+    return hi, lo, float(words[mp * n2p])
+
+
+def _n_quads(N):
+    """Quads before the padding: the energy quad is the last of them."""
+    return sum((d + 4) // 4 for d in range(N)) + (N + 3) // 4 + 1
 
 
 @pytest.mark.parametrize("N,P,A,X,precision,full", [(12, 64, 4, 3, 32, True), (64, 8, 8, 41, 64, True),
@@ -96,8 +104,8 @@ def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
            for k, v in (("qq", qq), ("l", lin), ("e", en))}
     t_q = torch.as_tensor(q).cuda().contiguous()
     nbp = int(lib.pbr_tc_potential_packed_floats(N, A))
-    mp = nbp // (2 * n2p)
-    assert mp == a2p
+    mp = (nbp - 4) // n2p
+    assert mp == a2p and nbp == a2p * n2p + 4
     bp = torch.full((nbp,), float("nan"), dtype=torch.float32, device="cuda")
     vq = torch.full((X * P, a2p), float("nan"), dtype=torch.float32, device="cuda")
     st = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -111,10 +119,17 @@ def test_tc_potential_matches_fp64(N, P, A, X, precision, full):
     rows = q.astype(np.float64).transpose(0, 2, 1).reshape(X * P, N)
     a_op, B = _expected_operands(N, A2, qq, lin, en, rows)
     assert B.shape[1] == n2p
-    # packed operands: hi + lo reproduce the FP32 couplings in the documented layout, padding zero
-    hi, lo = _unpack(bp.double().cpu().numpy(), mp, n2p)
-    assert np.allclose((hi + lo)[:A2], B.astype(np.float32), rtol=5e-7, atol=0)
-    assert not (hi + lo)[A2:].any()
+    # packed operands: (hi + lo) / 2^s_B reproduce the FP32 couplings in the documented layout;
+    # the first padding row holds 1 at the energies' column, the rest of the padding is zero
+    hi, lo, scale = _unpack(bp, mp, n2p)
+    assert scale > 0 and np.log2(scale) == np.round(np.log2(scale))
+    B32 = B.astype(np.float32).astype(np.float64)
+    assert np.max(np.abs(B32) * scale) < 2.0 ** 14
+    assert np.allclose((hi + lo)[:A2] / scale, B32, rtol=1e-6, atol=1e-7 * np.abs(B32).max())
+    unit = np.zeros(n2p)
+    unit[4 * (_n_quads(N) - 1)] = 1.0
+    assert np.array_equal((hi + lo)[A2], unit)
+    assert not (hi + lo)[A2 + 1:].any()
     ref = a_op @ B.T
     bound = np.abs(a_op) @ np.abs(B.T)
     got = vq.double().cpu().numpy()
