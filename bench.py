@@ -812,7 +812,7 @@ def mma_rates(args):
         for M in (128, 64):
             for N in (16, 32, 64, 80, 96, 128, 160, 256):
                 for nacc in (1, 2, 4):
-                    for at in ((0, 1) if (fmt == 2 and M == 128) else (0,)):
+                    for at in ((0, 1) if M == 128 else (0,)):
                         if nacc * N + (16 if at else 0) > 512:
                             continue
                         r, c = ctypes.c_double(), ctypes.c_double()
@@ -824,15 +824,16 @@ def mma_rates(args):
 
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
-    each, one persistent launch per surface count, autotuned tile budget, captured in a CUDA graph."""
+    each, one persistent launch per row-team group or register-chunk launches per model, the form
+    and tile budget autotuned per surface count, captured in a CUDA graph."""
     import torch
     from pibronic_gb300 import synthetic
     from pibronic_gb300.batch import ModelBatch, autotune
     count, X = args.batch_models, args.batch_samples
     preps = synthetic.batch_models(count=count, seed=3)
     seeds = list(range(1, count + 1))
-    budget, times = autotune(preps, seeds, X_probe=2048)
-    mb = ModelBatch(preps, [X] * count, seeds, smem_budget=budget)
+    budgets, times = autotune(preps, seeds, X_probe=16384)
+    mb = ModelBatch(preps, [X] * count, seeds, smem_budget=budgets)
     mb.capture()
     mb.replay()
     ts = []
@@ -844,7 +845,10 @@ def batched_leg(args):
     W = sum(flops_per_sample(p.A, p.N, p.P) for p in preps) * X
     return {"workload": f"{count} models, A~U{{2..8}}, N~U{{3..20}}, P~U{{8..256}}, T~U[100,500]K, {X} samples each",
             "samples_per_s": count * X / t, "ms_per_pass": 1e3 * t, "launch_groups": mb.groups,
-            "smem_budget_bytes": budget, "autotune_ms": {str(k): 1e3 * v for k, v in times.items()},
+            "chosen_budget_bytes": {str(a): ("register chunks" if b < 0 else b) for a, b in budgets.items()},
+            "autotune_ms": {str(a): {("register chunks" if b < 0 else str(b)): (None if v is None else 1e3 * v)
+                                     for b, v in tv.items()} for a, tv in times.items()},
+            "autotune_feasible_per_group": {str(a): sum(v is not None for v in tv.values()) for a, tv in times.items()},
             "algorithmic_tflops": W / t / 1e12,
             "median_ess_per_sample": statistics.median(e["ESS"] / X for e in ests),
             "finite": bool(int(mb.status.item()) == 0)}

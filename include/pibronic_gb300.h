@@ -122,7 +122,7 @@ int pbr_sample_eval(const pbr_model* model, uint64_t seed, uint64_t offset, int6
 /*
  * The same block evaluation with the potential V(q) built on the tensor cores, for large N
  * (precision 32 only): per chunk of samples the sampler writes q (into out->q_out when given,
- * else into scratch), the tcgen05 GEMM (TF32, hi/lo split, three MMAs per K step) writes V for
+ * else into scratch), the tcgen05 GEMM (FP16, hi/lo split, three MMAs per K step) writes V for
  * every (sample, bead) row, and the row-team kernel evaluates the chunk from q and that V.  Draws the same samples as pbr_sample_eval for the same seed and
  * offset.  scratch (256-byte aligned, scratch_bytes long) bounds the chunk:
  * pbr_sample_eval_tc_scratch(model, chunk) is the size for a chunk of that many samples; a
@@ -142,19 +142,22 @@ int pbr_eval_q_tc(const pbr_model* model, const float* q, int64_t X, const pbr_o
 /*
  * Many independent models in one launch per surface count (the batched configuration): every
  * model keeps its own sizes, temperature, seed, counter offset and outputs.  pbr_batch_pack fills
- * a host blob of pbr_batch_blob_bytes(n) bytes (tile shapes per model within smem_budget bytes of
- * shared memory, 0 = the maximum; a model whose one-sample tile exceeds the budget takes the
- * maximum instead; models grouped by surface count and series order; grid_cap
- * limits the persistent grid, 0 = occupancy x SMs); the caller copies it to a device buffer of the
- * same size; pbr_sample_eval_batch launches one persistent row-team kernel per group, CTAs taking
- * the concatenated tiles round-robin, except that groups of up to 4 surfaces (whose models all
- * leave the kernel form to the library or ask for register chunks) run one register-chunk launch
- * per model, the faster form there.  All models need precision 32.  The launches can be captured
- * in a CUDA graph (the blob holds everything they read).
+ * a host blob of pbr_batch_blob_bytes(n) bytes; smem_budgets (nullable; entries 0..8, indexed by
+ * the surface count) chooses each group's kernel form and tile shape: < 0 one register-chunk
+ * launch per model (up to 4 surfaces, the faster form there as a rule), 0 the row-team form with
+ * tiles sized for the whole shared memory, > 0 the row-team form with tiles within that many
+ * bytes (a model whose one-sample tile exceeds the budget takes the whole shared memory instead);
+ * a null table means register chunks up to 4 surfaces and whole-memory row-team tiles beyond.
+ * Models group by surface count and series order (and at 5-6 surfaces by whether two tiles fit an
+ * SM); grid_cap limits the persistent grid, 0 = occupancy x SMs.  The caller copies the blob to a
+ * device buffer of the same size; pbr_sample_eval_batch launches one persistent row-team kernel
+ * per row-team group, CTAs taking the concatenated tiles round-robin, and the register-chunk
+ * launches of the other groups.  All models need precision 32.  The launches can be captured in a
+ * CUDA graph (the blob holds everything they read).
  */
 int64_t pbr_batch_blob_bytes(int32_t n_models);
 int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_t* offsets, const int64_t* X,
-                   const pbr_outputs* outs, int32_t n_models, int32_t smem_budget, int32_t grid_cap,
+                   const pbr_outputs* outs, int32_t n_models, const int32_t* smem_budgets, int32_t grid_cap,
                    void* host_blob);
 int pbr_sample_eval_batch(const void* host_blob, const void* device_blob, void* stream);
 int32_t pbr_batch_groups(const void* host_blob);
@@ -386,17 +389,21 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
 
 /*
  * The diabatic potential alone (the middle stage of pbr_sample_eval_tc), for tests and custom
- * pipelines: V(q) = E + sum_j L_j q_j + sum_{d >= e} Qp_de q_d q_e as one tcgen05 GEMM (TF32 hi/lo
- * split, three MMAs per K step, FP32 accumulation in TMEM).  K is laid out in quads of four
- * columns (d, e0..e0+3) over the bead row's slots s = [q_0..q_{N-1}, 0 up to NA = N rounded up to
- * 4, 1, 0, 0, 0]: quads (d < N, e0 = 0, 4, .. <= d) hold the pairs e <= d, quads (NA, j0) the
- * linear terms, quad (NA, NA) the energies, quads (NA + 1, NA) pad to a multiple of 32.
+ * pipelines: V(q) = E + sum_j L_j q_j + sum_{d >= e} Qp_de q_d q_e as one tcgen05 GEMM
+ * (kind::f16: FP16 hi/lo split of both operands after exact power-of-two scaling of each bead row
+ * and of the couplings, three MMAs per K step of 16, FP32 accumulation in TMEM, about 22 bits
+ * per product).  K is laid out in quads of four columns (d, e0..e0+3) over the bead row's slots
+ * s = [q_0..q_{N-1}, 0 up to NA = N rounded up to 4, 1, 0, 0, 0]: quads (d < N, e0 = 0, 4, .. <= d)
+ * hold the pairs e <= d, quads (NA, j0) the linear terms, quad (NA, NA) the energies, quads
+ * (NA + 1, NA) pad to a multiple of 64.
  * pbr_tc_potential_dims gives the padded K extent n2p and the column count a2p (A(A+1)/2 rounded up
  * to 16).  pbr_tc_pack_potential turns vib_qq [N(N+1)/2][A(A+1)/2], vib_l [N][A(A+1)/2] and vib_e
  * [A(A+1)/2] (FP32 or FP64 as precision says; vib_l and vib_e nullable = zero) into b_packed
- * (pbr_tc_potential_packed_floats(N, A) = 2 * a2p * n2p floats, 16-byte aligned): per stage of 32
- * K columns, the TF32 hi part then the lo part, each a2p rows x 8 cores of 4 columns, core (row r,
- * core c) at ((r/8)*8 + c)*8 + r%8 in 16-byte units.
+ * (pbr_tc_potential_packed_floats(N, A) = a2p * n2p + 4 32-bit words, 16-byte aligned): per stage
+ * of 64 K columns, the FP16 hi part then the lo part of the couplings times 2^s_B, each a2p rows x
+ * 8 cores of 8 columns, core (row r, core c) at ((r/8)*8 + c)*8 + r%8 in 16-byte units; row
+ * A(A+1)/2 (the first padding row) holds 1 at the energies' column; then the largest |coupling|
+ * and the FP32 scale 2^s_B (the largest scaled coupling is below 2^14).
  * pbr_tc_potential writes vq [X * P][a2p] (FP32; row sample * P + bead, column pair_index(b, c))
  * from q [X][N][P] (FP32).  A <= 16, N <= 64.  Waits are bounded as in pbr_tc_gemm.  Replaces
  * pimc.py:1145-1150 (V of diagonalize_coupling_matrix).
@@ -404,7 +411,7 @@ int pbr_tc_gemm(int32_t fmt, const void* A, const void* B, float* C, int32_t M, 
 /* Tensor-pipe rate: one CTA per SM issues reps back-to-back tcgen05.mma from one thread --
  * fmt 2: kind::tf32, M x N x 8; fmt 1: kind::f16 with BF16 operands, M x N x 16 (M 64 or 128,
  * 16 <= N <= 256) -- round-robin over nacc (1..4) independent TMEM accumulators, A from shared
- * memory or (a_tmem = 1, TF32, M = 128) from TMEM; *tflops is the whole-GPU rate,
+ * memory or (a_tmem = 1, M = 128) from TMEM; *tflops is the whole-GPU rate,
  * *cycles_per_mma the issuing thread's cycles per instruction.  scratch: 16 bytes of the caller's
  * device memory, 8-byte aligned (the cycle count and the kernel's wait flag).  Synchronizes the
  * stream to read the result (a measurement, not a path entry point).  No counterpart in the

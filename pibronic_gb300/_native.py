@@ -113,7 +113,7 @@ def _declare(lib):
         "pbr_flow_weights": (C.c_int, [vp, vp, vp, vp, i64, vp, vp]),
         "pbr_adam": (C.c_int, [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, vp, vp]),
         "pbr_batch_blob_bytes": (i64, [i32]),
-        "pbr_batch_pack": (C.c_int, [vp, vp, vp, vp, vp, i32, i32, i32, vp]),
+        "pbr_batch_pack": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, i32, vp]),
         "pbr_sample_eval_batch": (C.c_int, [vp, vp, vp]),
         "pbr_batch_groups": (i32, [vp]),
         "pbr_reduce_terms_segments": (C.c_int, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp]),

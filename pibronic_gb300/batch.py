@@ -4,9 +4,10 @@ Each model keeps its own sizes (A, N, P), temperature, seed, counter offset and 
 ``ModelBatch.run`` evaluates all of them with ``pbr_sample_eval_batch`` (CTAs take the
 concatenated sample tiles round-robin and reload a model's tables when the model changes) and
 ``reduce`` turns every model's samples into Z, E, Cv with jackknife errors by segmented device
-reductions.  ``capture`` records both in a CUDA graph for replay.  ``autotune`` picks the
-shared-memory budget that fixes every model's tile shape (samples per tile) by timing the whole
-batch on a small sample count.
+reductions.  ``capture`` records both in a CUDA graph for replay.  ``autotune`` picks, per
+surface count, the kernel form and the shared-memory budget that fixes the models' tile shape
+(samples per tile, hence CTAs per SM and, at 5-6 surfaces, the two-block build) by timing each
+surface-count group alone for every candidate on a small sample count.
 """
 from __future__ import annotations
 
@@ -21,8 +22,26 @@ from .plan import DevicePlan
 from .stats import estimates_from_moments
 
 
+#: budget value that selects the per-model register-chunk launches (up to 4 surfaces)
+CHUNKS = -1
+MAX_A = 8
+
+
+def budget_table(smem_budget):
+    """Per-surface-count budgets (index = surface count) from None (register chunks up to 4
+    surfaces, whole shared memory beyond), an int (that budget for the row-team groups, register
+    chunks up to 4 surfaces) or a dict {A: budget} (missing entries as for None)."""
+    table = [0] + [CHUNKS if a <= 4 else 0 for a in range(1, MAX_A + 1)]
+    if isinstance(smem_budget, dict):
+        for a, b in smem_budget.items():
+            table[int(a)] = int(b)
+    elif smem_budget:
+        table = [0] + [CHUNKS if a <= 4 else int(smem_budget) for a in range(1, MAX_A + 1)]
+    return table
+
+
 class ModelBatch:
-    def __init__(self, preps, X, seeds, offsets=None, smem_budget=0, grid_cap=0):
+    def __init__(self, preps, X, seeds, offsets=None, smem_budget=None, grid_cap=0, plans=None):
         torch = _native.require_cuda()
         lib = _native.load()
         self.preps = list(preps)
@@ -32,7 +51,7 @@ class ModelBatch:
         self.offsets = np.zeros(M, dtype=np.uint64) if offsets is None else np.asarray(offsets, dtype=np.uint64)
         assert all(p.K == self.preps[0].K for p in self.preps), "one series order per batch"
         self.K = self.preps[0].K
-        self.plans = [DevicePlan(p, precision=32) for p in self.preps]
+        self.plans = list(plans) if plans is not None else [DevicePlan(p, precision=32) for p in self.preps]
         dev = torch.device("cuda", torch.cuda.current_device())
         self.seg = np.concatenate([[0], np.cumsum(self.X)]).astype(np.int64)
         total = int(self.seg[-1])
@@ -72,7 +91,9 @@ class ModelBatch:
         X = (ctypes.c_int64 * M)(*[int(v) for v in self.X])
         seeds = (ctypes.c_uint64 * M)(*[int(v) for v in self.seeds])
         offs = (ctypes.c_uint64 * M)(*[int(v) for v in self.offsets])
-        rc = lib.pbr_batch_pack(self._models, seeds, offs, X, self._outs, M, int(smem_budget), int(grid_cap),
+        self.budgets = budget_table(smem_budget)
+        table = (ctypes.c_int32 * len(self.budgets))(*self.budgets)
+        rc = lib.pbr_batch_pack(self._models, seeds, offs, X, self._outs, M, table, int(grid_cap),
                                 self._host_blob)
         _native.check(rc, "pbr_batch_pack")
         host = torch.frombuffer(bytearray(self._host_blob.raw), dtype=torch.uint8)
@@ -125,24 +146,43 @@ class ModelBatch:
         return [estimates_from_moments(m[i], j[i], self.T[i]) for i in range(len(self.preps))]
 
 
-def autotune(preps, seeds, X_probe=4096, budgets=(0, 150 * 1024, 110 * 1024, 72 * 1024), reps=3):
-    """Pick the shared-memory budget (hence every model's samples per tile and the CTAs per SM)
-    that evaluates the whole batch fastest on X_probe samples per model.  Returns (budget, times)."""
+def candidates(A):
+    """Kernel forms and shared-memory budgets tried for a surface count: up to 4 surfaces the
+    register-chunk launches and three row-team tile budgets, beyond that five row-team budgets
+    (at 5-6 surfaces the smaller ones let two tiles share an SM)."""
+    if A <= 4:
+        return (CHUNKS, 0, 110 * 1024, 72 * 1024)
+    return (0, 150 * 1024, 110 * 1024, 72 * 1024, 48 * 1024)
+
+
+def autotune(preps, seeds, X_probe=2048, reps=3):
+    """For each surface count of the batch, time that group's models alone (X_probe samples each)
+    under every candidate of ``candidates`` and keep the fastest.  Returns (budgets {A: budget},
+    times {A: {budget: seconds}}); a candidate the library refuses is recorded as None."""
     torch = _native.require_cuda()
-    times = {}
-    for b in budgets:
-        try:
-            mb = ModelBatch(preps, [X_probe] * len(preps), seeds, smem_budget=b)
-        except AssertionError:
-            continue
-        mb.run()
-        torch.cuda.synchronize()
-        best = float("inf")
-        for _ in range(reps):
-            t0 = time.perf_counter()
-            mb.run()
+    plans = [DevicePlan(p, precision=32) for p in preps]
+    budgets, times = {}, {}
+    for A in sorted({p.A for p in preps}):
+        idx = [i for i, p in enumerate(preps) if p.A == A]
+        sub = [preps[i] for i in idx]
+        subp = [plans[i] for i in idx]
+        subs = [seeds[i] for i in idx]
+        times[A] = {}
+        for b in candidates(A):
+            try:
+                mb = ModelBatch(sub, [X_probe] * len(sub), subs, smem_budget={A: b}, plans=subp)
+                mb.run()
+            except AssertionError:
+                times[A][b] = None
+                continue
             torch.cuda.synchronize()
-            best = min(best, time.perf_counter() - t0)
-        times[b] = best
-    budget = min(times, key=times.get)
-    return budget, times
+            best = float("inf")
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                mb.run()
+                torch.cuda.synchronize()
+                best = min(best, time.perf_counter() - t0)
+            times[A][b] = best
+        ok = {b: t for b, t in times[A].items() if t is not None}
+        budgets[A] = min(ok, key=ok.get)
+    return budgets, times

@@ -269,11 +269,14 @@ int64_t pbr_batch_blob_bytes(int32_t n_models) {
 }
 
 int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_t* offsets, const int64_t* X,
-                   const pbr_outputs* outs, int32_t n_models, int32_t smem_budget, int32_t grid_cap,
+                   const pbr_outputs* outs, int32_t n_models, const int32_t* smem_budgets, int32_t grid_cap,
                    void* host_blob) {
     using namespace pbr;
     if (!models || !seeds || !offsets || !X || !outs || !host_blob || n_models < 1) return PBR_ERR_ARG;
-    const int budget = (smem_budget > 0 && smem_budget < kMaxSmem) ? smem_budget : kMaxSmem;
+    // per surface count: < 0 the register-chunk launches (up to 4 surfaces), 0 the whole shared
+    // memory, > 0 a shared-memory budget for the row-team tiles; no table: chunks up to 4
+    // surfaces, the whole shared memory beyond
+    auto budget_of = [&](int A) { return smem_budgets ? smem_budgets[A] : (A <= 4 ? -1 : 0); };
     auto* hdr = static_cast<BatchHeader*>(host_blob);
     auto* items = reinterpret_cast<TeamBatchItem*>(hdr + 1);
     std::memset(hdr, 0, sizeof(BatchHeader));
@@ -287,7 +290,9 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
             const int first = n;
             int64_t tiles = 0;
             int smem = 0;
-            bool chunked = A <= 4;
+            const int ba = budget_of(A);
+            const int budget = (ba > 0 && ba < kMaxSmem) ? ba : kMaxSmem;
+            bool chunked = A <= 4 && ba < 0;
             for (int i = 0; i < n_models; ++i) {
                 const pbr_model& m = models[i];
                 if (m.A != A || m.K != K) continue;

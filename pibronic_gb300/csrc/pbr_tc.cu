@@ -7,6 +7,7 @@
 // N % 16 == 0 (16 <= N <= 256), K a multiple of the stage depth.  Every wait is bounded: on a
 // timeout the CTA records PBR_ERR_CUDA in *status, skips the rest of its work, and still frees
 // its TMEM.
+#include <algorithm>
 #include <cstdint>
 
 #include <cuda_fp16.h>
@@ -668,18 +669,20 @@ __global__ void __launch_bounds__(kPotThreads, 1) tc_potential_kernel(
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
-// 2^s_B for the couplings: the largest |entry| of Qp [N2][A2], L [N][A2], E [A2] (L, E nullable)
-// times 2^s_B stays below 2^14 (1 when every entry is zero).  One block; written to *scale.
+// The largest |entry| of Qp [N2][A2], L [N][A2], E [A2] (L, E nullable) into *maxbits (the bits
+// of a non-negative float, which order like the floats; zeroed by the caller): a grid-stride
+// maximum per block, then one atomicMax per block.
 template <typename T>
-__global__ void tc_pack_scale_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en,
-                                     int N, int A2, float* __restrict__ scale) {
+__global__ void tc_pack_max_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en,
+                                   int N, int A2, unsigned int* __restrict__ maxbits) {
     __shared__ float red[32];
     const int64_t nq = static_cast<int64_t>(N) * (N + 1) / 2 * A2, nl = lin ? static_cast<int64_t>(N) * A2 : 0,
                   ne = en ? A2 : 0;
     float m = 0.f;
-    for (int64_t i = threadIdx.x; i < nq + nl + ne; i += blockDim.x) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nq + nl + ne;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const T x = i < nq ? qq[i] : (i < nq + nl ? lin[i - nq] : en[i - nq - nl]);
-        m = fmaxf(m, fabsf(static_cast<float>(x)));
+        m = fmaxf(m, fminf(fabsf(static_cast<float>(x)), 3.0e38f));
     }
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -687,20 +690,27 @@ __global__ void tc_pack_scale_kernel(const T* __restrict__ qq, const T* __restri
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < static_cast<int>(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
-        m = fminf(m, 3.0e38f);
-        *scale = m > 0.f ? fp16_range_scale(fmaxf(m, 1.0e-30f)) : 1.f;
+        atomicMax(maxbits, __float_as_uint(m));
     }
+}
+
+// 2^s_B from the largest |entry| m: m 2^s_B < 2^14 (1 when every entry is zero)
+__device__ __forceinline__ float coupling_scale(unsigned int maxbits) {
+    const float m = __uint_as_float(maxbits);
+    return m > 0.f ? fp16_range_scale(fmaxf(m, 1.0e-30f)) : 1.f;
 }
 
 // Qp [N2][A2], L [N][A2], E [A2] (FP32 or FP64; L and E nullable = zero), times 2^s_B -> FP16
 // hi / lo in the stage-major shared-memory core layout: stage s = [hi: A2P rows][lo: A2P rows],
 // each row's 64 K columns as 8 cores of 8, core (row r, column c) at ((r / 8) * 8 + c) * 8 + r % 8
 // (16 B units), column k of the core in half k % 8.  Row A2 holds 1 at the energies' K column.
+// tail[0] holds the largest |entry| (tc_pack_max_kernel); block 0 writes 2^s_B to tail[1].
 template <typename T>
 __global__ void tc_pack_kernel(const T* __restrict__ qq, const T* __restrict__ lin, const T* __restrict__ en, int N,
-                               int A2, int nst, int A2P, const float* __restrict__ scale, __half* __restrict__ out) {
+                               int A2, int nst, int A2P, unsigned int* __restrict__ tail, __half* __restrict__ out) {
     const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;      // (stage, row, k in stage)
-    const float sB = *scale;
+    const float sB = coupling_scale(tail[0]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) reinterpret_cast<float*>(tail)[1] = sB;
     const int kone = energy_column(N);
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -748,7 +758,8 @@ namespace pbr {
 
 int tc_quadratic_cols(int A) { return (A * (A + 1) / 2 + 15) / 16 * 16; }
 int tc_quadratic_kdim(int N) { return (quad_count(N) + kQuadsPerStage - 1) / kQuadsPerStage * kQStageK; }
-// FP16 hi and lo of A2P x K couplings (one 32-bit word per two), then 4 words: the scale 2^s_B
+// FP16 hi and lo of A2P x K couplings (one 32-bit word per two), then 4 words: the largest
+// |coupling| and the scale 2^s_B
 int64_t tc_packed_floats(int N, int A) {
     return static_cast<int64_t>(tc_quadratic_cols(A)) * tc_quadratic_kdim(N) + 4;
 }
@@ -780,7 +791,7 @@ int tc_quadratic_launch(const float* q, int64_t X, int N, int P, int A, const vo
     const int smem = L.total > 116 * 1024 ? L.total : 116 * 1024;
     const int grid = static_cast<int>(tiles < sms ? tiles : sms);
     const auto* bp = static_cast<const unsigned char*>(bpack);
-    const float* scale = reinterpret_cast<const float*>(bp + static_cast<int64_t>(A2P) * tc_quadratic_kdim(N) * 4);
+    const float* scale = reinterpret_cast<const float*>(bp + static_cast<int64_t>(A2P) * tc_quadratic_kdim(N) * 4) + 1;
     tc_potential_kernel<<<grid, kPotThreads, smem, stream>>>(q, X, N, P, nst, A2, A2P, nb, bp, scale, vq, ncols,
                                                                  status);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
@@ -795,20 +806,23 @@ int tc_pack_launch(const void* qq, const void* lin, const void* en, int precisio
     const int64_t n = static_cast<int64_t>(nst) * A2P * kQStageK;
     const int grid = static_cast<int>((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     auto* out = static_cast<__half*>(bpack);
-    // the scale word after the 2 x A2P x K FP16 values (A2P x K x 4 bytes)
-    float* scale = reinterpret_cast<float*>(static_cast<unsigned char*>(bpack) + static_cast<int64_t>(A2P) * nst *
-                                            kQStageK * 4);
+    // the two tail words after the 2 x A2P x K FP16 values (A2P x K x 4 bytes)
+    auto* tail = reinterpret_cast<unsigned int*>(static_cast<unsigned char*>(bpack) + static_cast<int64_t>(A2P) * nst *
+                                                 kQStageK * 4);
+    const int64_t nin = static_cast<int64_t>(N) * (N + 1) / 2 * A2 + static_cast<int64_t>(N + 1) * A2;
+    const int mgrid = static_cast<int>(std::min<int64_t>((nin + 255) / 256, 304));
+    if (cudaMemsetAsync(tail, 0, sizeof(unsigned int), stream) != cudaSuccess) return PBR_ERR_CUDA;
     if (precision == 32) {
-        tc_pack_scale_kernel<float><<<1, 1024, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
-                                                            static_cast<const float*>(en), N, A2, scale);
+        tc_pack_max_kernel<float><<<mgrid, 256, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
+                                                             static_cast<const float*>(en), N, A2, tail);
         tc_pack_kernel<float><<<grid, 256, 0, stream>>>(static_cast<const float*>(qq), static_cast<const float*>(lin),
-                                                        static_cast<const float*>(en), N, A2, nst, A2P, scale, out);
+                                                        static_cast<const float*>(en), N, A2, nst, A2P, tail, out);
     } else if (precision == 64) {
-        tc_pack_scale_kernel<double><<<1, 1024, 0, stream>>>(static_cast<const double*>(qq),
-                                                             static_cast<const double*>(lin),
-                                                             static_cast<const double*>(en), N, A2, scale);
+        tc_pack_max_kernel<double><<<mgrid, 256, 0, stream>>>(static_cast<const double*>(qq),
+                                                              static_cast<const double*>(lin),
+                                                              static_cast<const double*>(en), N, A2, tail);
         tc_pack_kernel<double><<<grid, 256, 0, stream>>>(static_cast<const double*>(qq), static_cast<const double*>(lin),
-                                                         static_cast<const double*>(en), N, A2, nst, A2P, scale, out);
+                                                         static_cast<const double*>(en), N, A2, nst, A2P, tail, out);
     } else {
         return PBR_ERR_ARG;
     }
@@ -845,8 +859,8 @@ int pbr_tc_potential(const float* q, int64_t X, int32_t N, int32_t P, int32_t A,
 
 // ---------------------------------------------------------------------------------------------
 // Tensor-pipe rate probe: each CTA (one per SM) issues `reps` back-to-back tcgen05.mma (kind::tf32,
-// M x N x 8, or kind::f16 with BF16 operands, M x N x 16; operands zeros in shared memory, or the
-// TF32 A operand in TMEM) from one thread, round-robin over nacc independent TMEM accumulators,
+// M x N x 8, or kind::f16 with 16-bit operands, M x N x 16; operands zeros in shared memory, or the
+// A operand in TMEM) from one thread, round-robin over nacc independent TMEM accumulators,
 // commits once and waits (bounded).  Reports the issuing thread's cycles per MMA and the
 // whole-GPU TF/s: the denominator the potential GEMM is held against, and the evidence for what
 // an instruction costs (its shape, its operand type, its accumulator dependencies).
@@ -896,7 +910,8 @@ __global__ void tc_rate_kernel(int fmt, int M, int N, int nacc, int a_tmem, int 
         for (int i = 0; i < reps; ++i) {
             const uint32_t d = tmem + static_cast<uint32_t>(acc * N);
             const uint32_t accumulate = i >= nacc ? 1u : 0u;
-            if (fmt == 1) mma_issue<1>(d, da, db, idesc, accumulate);
+            if (fmt == 1 && a_tmem) mma_f16_ts(d, ta, db, idesc, accumulate);
+            else if (fmt == 1) mma_issue<1>(d, da, db, idesc, accumulate);
             else if (a_tmem) mma_tf32_ts(d, ta, db, idesc, accumulate);
             else mma_issue<2>(d, da, db, idesc, accumulate);
             if (++acc == nacc) acc = 0;
@@ -918,7 +933,7 @@ __global__ void tc_rate_kernel(int fmt, int M, int N, int nacc, int a_tmem, int 
 extern "C" int pbr_tc_mma_rate(int32_t fmt, int32_t M, int32_t N, int32_t nacc, int32_t a_tmem, int32_t reps,
                                void* scratch, double* tflops, double* cycles_per_mma, void* stream) {
     if ((fmt != 1 && fmt != 2) || (M != 64 && M != 128) || N < 16 || N > 256 || N % 16 != 0 || nacc < 1 ||
-        nacc > 4 || nacc * N + (a_tmem ? 16 : 0) > 512 || (a_tmem && (fmt != 2 || M != 128)) || reps < 1 ||
+        nacc > 4 || nacc * N + (a_tmem ? 16 : 0) > 512 || (a_tmem && M != 128) || reps < 1 ||
         reps > (1 << 20) || !tflops || !cycles_per_mma || !scratch || (reinterpret_cast<uintptr_t>(scratch) & 7) != 0)
         return PBR_ERR_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -105,3 +105,39 @@ def test_batch_dispatch_forms_match_single_model_runs():
             single = evaluate_device(DevicePlan(prep, precision=32, variant=variant), X[i], seed=seeds[i], offset=0)
             for k in ("s_rho", "s_g", "s_gp", "s_gm"):
                 assert torch.allclose(mb.out[k][sl], single[k], rtol=2e-4, atol=0), (shapes[i], variant, k)
+
+
+def test_autotuner_times_every_candidate_per_surface_count_and_its_choice_is_exact():
+    """autotune times each surface-count group under every candidate form / tile budget (at least
+    three feasible per group), and a batch packed with its choices (and with every candidate
+    forced on all groups) reproduces the single-model runs."""
+    from pibronic_gb300 import constants, synthetic
+    from pibronic_gb300.batch import ModelBatch, autotune, candidates
+    from pibronic_gb300.plan import DevicePlan, PreparedModels
+    from pibronic_gb300.pimc import evaluate_device
+    shapes = [(2, 5, 24), (3, 6, 32), (5, 16, 48), (6, 20, 128), (7, 8, 40)]
+    preps = []
+    for i, (A, N, P) in enumerate(shapes):
+        m = synthetic.make_coupled_model(A, N, 3000 + i, sd_quadratic=0.0005)
+        beta = constants.beta(200.0 + 30 * i)
+        preps.append(PreparedModels(m, synthetic.diagonal_of(m), P, beta=beta, delta_beta=1e-4 * beta))
+    seeds = [41 + i for i in range(len(shapes))]
+    budgets, times = autotune(preps, seeds, X_probe=512, reps=2)
+    assert sorted(budgets) == sorted({s[0] for s in shapes})
+    for A, tv in times.items():
+        assert set(tv) == set(candidates(A))
+        assert sum(v is not None for v in tv.values()) >= 3, (A, tv)
+        assert budgets[A] in tv and tv[budgets[A]] is not None
+    X = [400 + 11 * i for i in range(len(shapes))]
+    singles = [evaluate_device(DevicePlan(p, precision=32, variant=2), X[i], seed=seeds[i], offset=0)
+               for i, p in enumerate(preps)]
+    tables = [budgets] + [{A: b for A in budgets} for b in (0, 72 * 1024, 48 * 1024)]
+    for table in tables:
+        mb = ModelBatch(preps, X, seeds, smem_budget=table)
+        mb.run()
+        torch.cuda.synchronize()
+        assert int(mb.status.item()) == 0
+        for i in range(len(preps)):
+            sl = slice(int(mb.seg[i]), int(mb.seg[i + 1]))
+            for k in ("s_rho", "s_g", "s_gp", "s_gm"):
+                assert torch.allclose(mb.out[k][sl], singles[i][k], rtol=2e-4, atol=0), (table, shapes[i], k)

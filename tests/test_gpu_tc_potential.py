@@ -63,7 +63,7 @@ def _expected_operands(N, A2, qq, lin, en, q_rows):
 
 def _unpack(bp, mp, n2p):
     """b_packed (stages of 64 K columns, FP16 hi then lo, mp rows each, in the core layout; then
-    the FP32 scale 2^s_B) -> hi, lo [mp][n2p] (FP64) and the scale."""
+    the largest |coupling| and the FP32 scale 2^s_B) -> hi, lo [mp][n2p] (FP64) and the scale."""
     words = bp.cpu().numpy()
     h = words[:mp * n2p].view(np.float16).astype(np.float64)
     nst = n2p // 64
@@ -76,7 +76,7 @@ def _unpack(bp, mp, n2p):
         for part, dst in ((0, hi), (1, lo)):
             blk = h[base + part * mp * 64: base + (part + 1) * mp * 64]
             dst[:, st * 64: (st + 1) * 64] = blk[idx]
-    return hi, lo, float(words[mp * n2p])
+    return hi, lo, float(words[mp * n2p + 1])
 
 
 def _n_quads(N):

@@ -73,14 +73,15 @@ def _fake_models(shapes, variant=0):
     return models, outs
 
 
-def _pack(lib, shapes, variant=0, budget=0):
+def _pack(lib, shapes, variant=0, budget=None):
     M = len(shapes)
     models, outs = _fake_models(shapes, variant)
     seeds = (ctypes.c_uint64 * M)(*range(1, M + 1))
     offs = (ctypes.c_uint64 * M)()
     X = (ctypes.c_int64 * M)(*([1000] * M))
     blob = ctypes.create_string_buffer(int(lib.pbr_batch_blob_bytes(M)))
-    rc = lib.pbr_batch_pack(models, seeds, offs, X, outs, M, budget, 0, blob)
+    budgets = None if budget is None else (ctypes.c_int32 * 9)(*budget)
+    rc = lib.pbr_batch_pack(models, seeds, offs, X, outs, M, budgets, 0, blob)
     return rc, blob
 
 
@@ -107,3 +108,25 @@ def test_batch_packing_rejects_bad_models():
     assert rc == _native.PBR_ERR_ARG
     rc, _ = _pack(lib, [(9, 4, 16)])              # more surfaces than the row-team form holds
     assert rc != 0
+
+
+def test_batch_packing_follows_the_per_surface_count_budgets():
+    """A negative budget keeps a group of up to 4 surfaces on the register-chunk launches, 0 or a
+    positive budget puts it on the row-team form; a budget smaller than one model's one-sample
+    tile makes that model take the whole shared memory instead of failing the pack; at 5-6
+    surfaces a small budget moves a model into the two-block class (another group)."""
+    from pibronic_gb300 import build, _native
+    lib = _native.load(build.build())
+    shapes = [(2, 4, 16), (4, 12, 64), (6, 20, 128), (6, 10, 32)]
+    chunks = [0, -1, -1, -1, -1, 0, 0, 0, 0]
+    rc, blob = _pack(lib, shapes, budget=chunks)
+    assert rc == 0 and lib.pbr_batch_groups(blob) == 4
+    teams = [0, 0, 0, 0, 0, 0, 0, 0, 0]
+    rc, blob = _pack(lib, shapes, budget=teams)
+    assert rc == 0 and lib.pbr_batch_groups(blob) == 4
+    tiny = [0, 4096, 4096, 4096, 4096, 4096, 4096, 4096, 4096]     # below every one-sample tile
+    rc, blob = _pack(lib, shapes, budget=tiny)
+    assert rc == 0
+    small = [0, -1, -1, -1, -1, 72 * 1024, 72 * 1024, 0, 0]
+    rc, blob = _pack(lib, [(6, 20, 128), (6, 20, 64)], budget=small)
+    assert rc == 0 and lib.pbr_batch_groups(blob) >= 1
