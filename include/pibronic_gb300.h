@@ -342,6 +342,21 @@ int pbr_flow_apply(const float* q, const float* y, const float* y_new, int64_t X
 int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64_t X, float* y,
                            double* logdet, const pbr_flow_save* save, void* stream);
 
+/* The same layer in the sampling direction (+1) on the tensor cores: per tile of 128 samples the
+ * three products as tcgen05.mma kind::f16 GEMMs with BF16 weights and activations and FP32
+ * accumulation in TMEM; the coupling update y_B e^s + t and logdet += sum s in FP32 (logdet FP64).
+ * The log-determinant is exactly that of the map applied (y_A passes unchanged), so the proposal
+ * density stays exact for the BF16 network.  pbr_flow_tc_pack converts the layer's FP32 weights
+ * into `packed` (pbr_flow_tc_packed_bytes(D, I, J, H) bytes, 16-byte aligned; -1 when the shape
+ * is unsupported: H a multiple of 32 up to 128, I <= 128, 2J <= 256, and the packed weights with
+ * one 128-sample tile of y within 227 KB of shared memory); repack after the weights
+ * change.  status (nullable) gets PBR_ERR_CUDA if a bounded wait gave up.  No counterpart in the
+ * reference. */
+int64_t pbr_flow_tc_packed_bytes(int32_t D, int32_t I, int32_t J, int32_t H);
+int pbr_flow_tc_pack(const pbr_flow_layer* layer, void* packed, void* stream);
+int pbr_flow_tc_forward(const pbr_flow_layer* layer, const void* packed, int64_t X, float* y, double* logdet,
+                        int32_t* status, void* stream);
+
 /* Back-propagation through one layer of the -1 direction using its saved activations:
  * gy [X][D] holds dL/d(output) on entry, dL/d(input) on exit; rt [X] the per-sample weights of
  * the log-det term; writes g_o [X][2J], g_z2 [X][H], g_z1 [X][H] for the weight gradients. */

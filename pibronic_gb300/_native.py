@@ -30,6 +30,7 @@ EXPORTED = (
     "pbr_reduce_terms", "pbr_reduce_jackknife", "pbr_reduce_blocks", "pbr_fma_probe",
     "pbr_reduce_terms_static", "pbr_reduce_terms_static_max_samples",
     "pbr_flow_prepare", "pbr_flow_apply", "pbr_flow_layer_forward", "pbr_flow_layer_backward",
+    "pbr_flow_tc_packed_bytes", "pbr_flow_tc_pack", "pbr_flow_tc_forward",
     "pbr_gemm_tn_acc", "pbr_gemm_tn_scratch", "pbr_colsum", "pbr_flow_base", "pbr_flow_weights",
     "pbr_adam", "pbr_batch_blob_bytes", "pbr_batch_pack", "pbr_sample_eval_batch", "pbr_batch_groups",
     "pbr_reduce_terms_segments", "pbr_reduce_jackknife_segments", "pbr_reduce_segments_scratch",
@@ -106,6 +107,9 @@ def _declare(lib):
                                              C.POINTER(PbrFlowSave), vp]),
         "pbr_flow_layer_backward": (C.c_int, [C.POINTER(PbrFlowLayer), i64, vp, vp,
                                               C.POINTER(PbrFlowSave), vp, vp, vp, vp]),
+        "pbr_flow_tc_packed_bytes": (i64, [i32, i32, i32, i32]),
+        "pbr_flow_tc_pack": (C.c_int, [C.POINTER(PbrFlowLayer), vp, vp]),
+        "pbr_flow_tc_forward": (C.c_int, [C.POINTER(PbrFlowLayer), vp, i64, vp, vp, vp, vp]),
         "pbr_gemm_tn_acc": (C.c_int, [vp, vp, i64, i32, i32, C.c_float, vp, vp, vp, vp]),
         "pbr_gemm_tn_scratch": (i64, [i64, i32, i32]),
         "pbr_colsum": (C.c_int, [vp, i64, i32, vp, vp]),

@@ -98,6 +98,13 @@ class FlowProposal:
         self.nu = self._flat[self._nu_off:self._nu_off + A]
         self._t_log_w = torch.as_tensor(self.log_w, dtype=torch.float32, device=dev)
         self._adam = None
+        # the sampling direction on the tensor cores (BF16 weights, FP32 coupling and log-det)
+        # where every layer's shape allows it; sample_and_evaluate uses it by default
+        lib = _lib()
+        self._tc_bytes = [int(lib.pbr_flow_tc_packed_bytes(self.D, int(a.numel()), int(b.numel()), hidden))
+                          for a, b in self.idx]
+        self.sample_tc = all(n > 0 for n in self._tc_bytes)
+        self._tc_packs = None
         self._step = torch.zeros(1, dtype=torch.int32, device=dev)       # Adam's step count
 
     def _views(self, flat, l):
@@ -145,6 +152,27 @@ class FlowProposal:
                                                         _native.stream_handle()), "flow forward")
         return yo, ld
 
+    def forward_tc(self, y):
+        """The sampling direction on the tensor cores: y' and log|det dy'/dy| (FP64) of the
+        BF16 network (the weights are converted on every call, so they follow training)."""
+        torch = _native.require_cuda()
+        assert self.sample_tc, "a layer shape the tensor-core form does not hold"
+        lib = _lib()
+        p = _native.ptr
+        sh = _native.stream_handle()
+        if self._tc_packs is None:
+            self._tc_packs = [torch.empty(n, dtype=torch.uint8, device=self.dev) for n in self._tc_bytes]
+        yo = y.clone()
+        ld = torch.zeros(y.shape[0], dtype=torch.float64, device=self.dev)
+        st = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        for l in range(self.layers):
+            layer = self.layer_struct(l)
+            _native.check(lib.pbr_flow_tc_pack(layer, p(self._tc_packs[l]), sh), "flow tc pack")
+            _native.check(lib.pbr_flow_tc_forward(layer, p(self._tc_packs[l]), y.shape[0], p(yo), p(ld), p(st), sh),
+                          "flow tc forward")
+        self._tc_status = st
+        return yo, ld
+
     def inverse(self, y, saves=None):
         torch = _native.require_cuda()
         yo = y.clone()
@@ -178,9 +206,10 @@ class FlowProposal:
         torch = _native.require_cuda()
         return (torch.as_tensor(self.log_k, dtype=torch.float32, device=self.dev) + self.log_pi()).contiguous()
 
-    def sample_and_evaluate(self, X, seed, offset=0, keep=False):
+    def sample_and_evaluate(self, X, seed, offset=0, keep=False, tc=None):
         """Draw X proposal samples and evaluate them: returns CUDA tensors s_q (proposal density in
-        the scale of g's outputs), s_g, s_gp, s_gm, and with keep also x, y(x)."""
+        the scale of g's outputs), s_g, s_gp, s_gm, and with keep also x, y(x).  tc (default: every
+        layer's shape allows it) moves the samples with the tensor-core layers."""
         torch = _native.require_cuda()
         from .pimc import evaluate_device
         lib = _lib()
@@ -190,7 +219,8 @@ class FlowProposal:
         _native.check(lib.pbr_sample_q(m, int(seed), int(offset), X, p(q), None, _native.stream_handle()),
                       "sample_q")
         y, U = self.prepare(q)
-        yn, logdet = self.forward(y)
+        use_tc = self.sample_tc if tc is None else tc
+        yn, logdet = self.forward_tc(y) if use_tc else self.forward(y)
         lse = torch.empty(X, dtype=torch.float64, device=self.dev)
         lpa = self.log_pi_abs()
         _native.check(lib.pbr_flow_base(p(y), None, X, self.D, self.A, p(self.t_mu), p(lpa), None, None,
@@ -202,8 +232,9 @@ class FlowProposal:
         s_q = torch.empty(X, dtype=torch.float64, device=self.dev)
         _native.check(lib.pbr_flow_weights(p(lse), p(U), p(logdet), p(out["log_scale"]), X, p(s_q),
                                            _native.stream_handle()), "flow weights")
+        status = torch.maximum(out["status"], self._tc_status) if use_tc else out["status"]
         res = {"s_q": s_q, "s_g": out["s_g"], "s_gp": out.get("s_gp"), "s_gm": out.get("s_gm"),
-               "status": out["status"]}
+               "status": status}
         if keep:
             res["x"] = x
             res["y"] = self.prepare(x)[0]

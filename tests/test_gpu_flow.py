@@ -1,6 +1,7 @@
 """GPU: the learned proposal's kernels against the numpy flow oracle (oracle/flow_oracle.py),
-the exactness of its density (unbiased estimates for any parameters, checked on a model with a
-closed-form answer), and what training gains over plain rho."""
+the tensor-core layers of the sampling direction against the FP32 ones, the exactness of the
+density (unbiased estimates for any parameters, checked on a model with a closed-form answer, with
+the tensor-core layers that sampling uses by default), and what training gains over plain rho."""
 import math
 
 import numpy as np
@@ -77,6 +78,33 @@ def test_layers_match_oracle(tmp_path, N, nsel, layers, hidden, X):
     yi, ldi = fl.inverse(yf)
     assert np.allclose(yi.cpu().numpy(), y.cpu().numpy(), atol=1e-4)
     assert np.allclose(ldi.cpu().numpy(), -ldf.cpu().numpy(), atol=1e-4)
+
+
+@pytest.mark.parametrize("N,nsel,layers,hidden,X", LAYER_CASES)
+def test_tensor_core_layers_follow_the_fp32_layers(tmp_path, N, nsel, layers, hidden, X):
+    """The BF16 tensor-core layers (sampling direction) against the FP32 layers on the same
+    weights: BF16 rounds the weights and activations to 8 bits, so y' and the log-determinant
+    follow the FP32 network to about 1e-2 of their scale, not to FP32 rounding.  With a zero head
+    the layers are the identity exactly."""
+    FS, data = _box(tmp_path, A=2, N=N, P=12, X=64)
+    fl = _flow(data, nsel=nsel, layers=layers, hidden=hidden, init_scale=0.5, seed=2)
+    # D = 192 at hidden 128: the weights and a 128-sample tile exceed the shared memory, and that
+    # proposal samples with the FP32 layers
+    assert fl.sample_tc == (fl.D <= 128)
+    if not fl.sample_tc:
+        return
+    y = torch.randn((X, fl.D), device="cuda")
+    yf, ldf = fl.forward(y)
+    yt, ldt = fl.forward_tc(y)
+    torch.cuda.synchronize()
+    assert int(fl._tc_status.item()) == 0
+    dy = float((yt - yf).abs().max() / (yf.abs().max() + 1.0))
+    dl = float((ldt - ldf).abs().max() / (ldf.abs().max() + 1.0))
+    print(f"N={N} nsel={nsel} layers={layers} H={hidden} X={X}: max |dy| {dy:.2e}, |dlogdet| {dl:.2e}")
+    assert dy < 3e-2 and dl < 3e-2, (dy, dl)
+    zero = _flow(data, nsel=nsel, layers=layers, hidden=hidden, init_scale=0.0, seed=2)
+    yz, ldz = zero.forward_tc(y)
+    assert torch.equal(yz, y) and not bool(ldz.abs().max() > 0)
 
 
 @pytest.mark.parametrize("N,nsel,layers,hidden,X", [(4, 3, 4, 32, 4096), (5, 3, 2, 128, 1000),
