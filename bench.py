@@ -834,6 +834,35 @@ def mma_rates(args):
     return 0
 
 
+def profile_flow(args):
+    """Profiling helper (no JSON line): the learned configuration's flow (A=6, N=20, P=128,
+    hidden 128, 8 layers): 20 training steps at batch 16384 on rho's weighted samples, then one
+    args.profile_flow-sample draw through the tensor-core sampling layers, for an ncu capture."""
+    import torch
+    from pibronic_gb300 import constants, pimc, synthetic
+    from pibronic_gb300.file_structure import FileStructure
+    from pibronic_gb300.flow import FlowProposal
+    from pibronic_gb300.pimc import evaluate_device
+    A, N, P, T = 6, 20, 128, 200.0
+    FS = FileStructure(tempfile.mkdtemp(prefix="pbr_pflow_"), 0, 0)
+    synthetic.write_model_pair(FS, A, N, args.learned_seeds[0], sd_offdiag=0.1)
+    data = pimc.BoxDataPM(1e-4 * constants.beta(T))
+    data.path_vib_model, data.path_rho_model = FS.path_vib_model, FS.path_rho_model
+    data.states, data.modes, data.beads, data.temperature = A, N, P, T
+    data.samples = data.block_size = 1000
+    data.blocks = 1
+    data.preprocess()
+    pl = evaluate_device(data.plan, 20 * 16384, seed=1, offset=0, want_q=True)
+    fl = FlowProposal(data.prepared, data.plan, nsel=3, layers=8, hidden=128, seed=0)
+    y, _ = fl.prepare(pl["q"])
+    fl.train(y, pl["s_g"] / pl["s_rho"], epochs=1, batch=16384, lr=1e-3)
+    out = fl.sample_and_evaluate(args.profile_flow, seed=5)
+    torch.cuda.synchronize()
+    assert int(out["status"].item()) == 0
+    print("profile-flow done", args.profile_flow)
+    return 0
+
+
 def batched_leg(args):
     """256 seeded models, A ~ U{2..8}, N ~ U{3..20}, P ~ U{8..256}, T ~ U[100, 500] K, 1e5 samples
     each, one persistent launch per row-team group or register-chunk launches per model, the form
@@ -891,11 +920,15 @@ def main():
     ap.add_argument("--profile-learned", type=int, default=0,
                     help="profiling helper: evaluate this many plain-rho samples of the learned "
                          "configuration's model twice, exit")
+    ap.add_argument("--profile-flow", type=int, default=0,
+                    help="profiling helper: 20 flow training steps, then this many tensor-core flow samples, exit")
     ap.add_argument("--mma-rates", action="store_true",
                     help="profiling helper: sweep the tcgen05 rate probe, print a table, exit")
     args = ap.parse_args()
     if args.mma_rates:
         return mma_rates(args)
+    if args.profile_flow > 0:
+        return profile_flow(args)
     if args.profile_large > 0:
         return profile_large(args)
     if args.profile_learned > 0:
