@@ -49,10 +49,10 @@ extern "C" {
  *   vib_l    [N * A(A+1)/2]     linear couplings, diagonal folded away (pimc.py:214)
  *   vib_qq   [N(N+1)/2 * A(A+1)/2]  for mode pair (d>=e): 1/2 (Q_de + Q_ed) if d>e, 1/2 Q_dd if d==e
  *   rho_cs, rho_th [N], rho_c [A_rho], rho_d [A_rho * N]   the sampling model at beta (order 0)
- *   ring_chol [3 * N * P]       per mode j, the bead precision of rho, 2 coth_j I - csch_j C
+ *   ring_chol [3 * P * N]       per mode j, the bead precision of rho, 2 coth_j I - csch_j C
  *                               (C the ring adjacency; pimc.py:402-404), factored L L^T: a_p =
  *                               1/L_pp, b_p = L_{p+1,p} (L_{P-1,P-2} at p = P-2), c_p = L_{P-1,p}
- *                               (p <= P-3), as arrays a[j][p], b[j][p], c[j][p].  The matrix is
+ *                               (p <= P-3), as bead-major arrays a[p][j], b[p][j], c[p][j].  The matrix is
  *                               cyclic tridiagonal, so L is bidiagonal plus a dense last row and
  *                               q - d = L^-T z (z standard normal) costs O(P) per mode.
  *   src_cdf  [A_rho]            cumulative normalised state weights       (pimc.py:343-350)

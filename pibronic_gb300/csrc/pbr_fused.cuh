@@ -198,81 +198,107 @@ __device__ __forceinline__ void jacobi_accumulate(T (&a)[A][A], T (&u)[A][A], in
 constexpr int kExpmMinA = 3;
 constexpr int kFlatPairsMinA = 4;
 
-// exp(-tau V) for a small symmetric V held in registers (FP32): V is shifted by its mean
-// eigenvalue (trace / A), scaled by 2^-s until ||tau (V - mean)||_inf <= 1/2, exponentiated by the
-// degree-8 Taylor polynomial (Paterson-Stockmeyer: C_0 + B^3 (C_1 + B^3 C_2), truncation < 1e-8)
-// and squared s times.  M = 2^(tl - n2) X with tl = -tau mean log2(e); returns n2, the power of two
-// taken out.  For symmetric V this is the matrix the reference forms from eigh (pimc.py:1197-1205).
+// index of entry (r, c) of a symmetric A x A matrix stored as its lower triangle (pair order)
+__host__ __device__ constexpr int sym_index(int r, int c) { return r >= c ? r * (r + 1) / 2 + c : c * (c + 1) / 2 + r; }
+
+// Z = X Y for symmetric X, Y that are polynomials in one matrix (so Z is symmetric): the lower
+// triangle only, each entry summed over m in order
 template <int A>
-__device__ __forceinline__ int expm_neg_tau(const float (&am)[A][A], float tau, float (&M)[A][A]) {
+__device__ __forceinline__ void sym_mul(const float (&X)[npair(A)], const float (&Y)[npair(A)], float (&Z)[npair(A)]) {
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c) {
+            float acc = 0.f;
+#pragma unroll
+            for (int m = 0; m < A; ++m) acc = fmaf(X[sym_index(r, m)], Y[sym_index(m, c)], acc);
+            Z[sym_index(r, c)] = acc;
+        }
+}
+
+// exp(-tau V) for a small symmetric V given as its lower triangle vp (pair order), in FP32
+// registers: V is shifted by its mean eigenvalue (trace / A), scaled by 2^-s until
+// ||tau (V - mean)||_inf <= 1/2, exponentiated by the degree-8 Taylor polynomial
+// (Paterson-Stockmeyer: C_0 + B^3 (C_1 + B^3 C_2), truncation < 1e-8) and squared s times.  Every
+// intermediate is a polynomial in B, hence symmetric, and is kept as its lower triangle (A(A+1)/2
+// registers and A^2 (A+1)/2 FMAs per product).  M = 2^(tl - n2) X with tl = -tau mean log2(e);
+// returns n2, the power of two taken out.  For symmetric V this is the matrix the reference forms
+// from eigh (pimc.py:1197-1205).
+// The lower triangle X of the scaled exponential and its factor: M = f X, f = 2^(tl - n2).
+template <int A>
+__device__ __forceinline__ int expm_neg_tau_packed(const float (&vp)[npair(A)], float tau, float (&X)[npair(A)],
+                                                   float& f) {
+    constexpr int NS = npair(A);
     float mean = 0.f;
 #pragma unroll
-    for (int i = 0; i < A; ++i) mean += am[i][i];
+    for (int i = 0; i < A; ++i) mean += vp[sym_index(i, i)];
     mean *= 1.f / float(A);
-    float B[A][A];
+    float B[NS];
+#pragma unroll
+    for (int r = 0; r < A; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c) B[sym_index(r, c)] = -tau * (vp[sym_index(r, c)] - (r == c ? mean : 0.f));
     float nrm = 0.f;
 #pragma unroll
     for (int r = 0; r < A; ++r) {
         float rs = 0.f;
 #pragma unroll
-        for (int c = 0; c < A; ++c) {
-            B[r][c] = -tau * (am[r][c] - (r == c ? mean : 0.f));
-            rs += fabsf(B[r][c]);
-        }
+        for (int c = 0; c < A; ++c) rs += fabsf(B[sym_index(r, c)]);
         nrm = fmaxf(nrm, rs);
     }
     int s = 0;
     while (nrm > 0.5f && s < 40) { nrm *= 0.5f; ++s; }
     const float sc = ldexpf(1.f, -s);
 #pragma unroll
-    for (int r = 0; r < A; ++r)
-#pragma unroll
-        for (int c = 0; c < A; ++c) B[r][c] *= sc;
-    auto mul = [](const float (&X)[A][A], const float (&Y)[A][A], float (&Z)[A][A]) {
-#pragma unroll
-        for (int r = 0; r < A; ++r)
-#pragma unroll
-            for (int c = 0; c < A; ++c) {
-                float acc = 0.f;
-#pragma unroll
-                for (int m = 0; m < A; ++m) acc = fmaf(X[r][m], Y[m][c], acc);
-                Z[r][c] = acc;
-            }
-    };
-    float B2[A][A], B3[A][A], T1[A][A], X[A][A];
-    mul(B, B, B2);
-    mul(B2, B, B3);
+    for (int i = 0; i < NS; ++i) B[i] *= sc;
+    float B2[NS], B3[NS], T1[NS];
+    sym_mul<A>(B, B, B2);
+    sym_mul<A>(B2, B, B3);
     constexpr float c3 = 1.f / 6.f, c4 = 1.f / 24.f, c5 = 1.f / 120.f, c6 = 1.f / 720.f, c7 = 1.f / 5040.f,
                     c8 = 1.f / 40320.f;
 #pragma unroll
     for (int r = 0; r < A; ++r)
 #pragma unroll
-        for (int c = 0; c < A; ++c) T1[r][c] = (r == c ? c6 : 0.f) + c7 * B[r][c] + c8 * B2[r][c];
-    mul(T1, B3, X);
+        for (int c = 0; c <= r; ++c) {
+            const int i = sym_index(r, c);
+            T1[i] = (r == c ? c6 : 0.f) + c7 * B[i] + c8 * B2[i];
+        }
+    sym_mul<A>(T1, B3, X);
 #pragma unroll
     for (int r = 0; r < A; ++r)
 #pragma unroll
-        for (int c = 0; c < A; ++c) T1[r][c] = X[r][c] + (r == c ? c3 : 0.f) + c4 * B[r][c] + c5 * B2[r][c];
-    mul(T1, B3, X);
+        for (int c = 0; c <= r; ++c) {
+            const int i = sym_index(r, c);
+            T1[i] = X[i] + (r == c ? c3 : 0.f) + c4 * B[i] + c5 * B2[i];
+        }
+    sym_mul<A>(T1, B3, X);
 #pragma unroll
     for (int r = 0; r < A; ++r)
 #pragma unroll
-        for (int c = 0; c < A; ++c) X[r][c] += (r == c ? 1.f : 0.f) + B[r][c] + 0.5f * B2[r][c];
+        for (int c = 0; c <= r; ++c) {
+            const int i = sym_index(r, c);
+            X[i] += (r == c ? 1.f : 0.f) + B[i] + 0.5f * B2[i];
+        }
     for (int i = 0; i < s; ++i) {
-        mul(X, X, T1);
+        sym_mul<A>(X, X, T1);
 #pragma unroll
-        for (int r = 0; r < A; ++r)
-#pragma unroll
-            for (int c = 0; c < A; ++c) X[r][c] = T1[r][c];
+        for (int j = 0; j < NS; ++j) X[j] = T1[j];
     }
     const float tl = -tau * mean * 1.4426950408889634f;
     const float n2 = floorf(tl);
-    const float f = exp2f(tl - n2);
+    f = exp2f(tl - n2);
+    return static_cast<int>(n2);
+}
+
+template <int A>
+__device__ __forceinline__ int expm_neg_tau(const float (&vp)[npair(A)], float tau, float (&M)[A][A]) {
+    float X[npair(A)], f;
+    const int n2 = expm_neg_tau_packed<A>(vp, tau, X, f);
 #pragma unroll
     for (int r = 0; r < A; ++r)
 #pragma unroll
-        for (int c = 0; c < A; ++c) M[r][c] = f * X[r][c];
-    return static_cast<int>(n2);
+        for (int c = 0; c < A; ++c) M[r][c] = f * X[sym_index(r, c)];
+    return n2;
 }
 
 // Compensated (Kahan) FP32 sum for the per-chunk log accumulators; plain sum in FP64.
@@ -334,26 +360,37 @@ __device__ __forceinline__ int draw_source(const pbr_model& m, uint64_t sg, uint
 // that draws through this function produces the same bits.  The distribution is rho's
 // N(d_src, Lambda^-1), the one the reference draws in normal modes.
 // one step of the back substitution: x_{P-1} = a z, else x_p = a_p (z_p - b_p x_{p+1} - c_p x_{P-1});
-// xnext <- x_p (and xlast <- x_p at p = P-1)
+// xnext <- x_p (and xlast <- x_p at p = P-1).  The product by a_p is rounded on its own (no
+// contraction into the q_p = x_p + d add that follows), so every caller gets the same bits.
+__device__ __forceinline__ float mul_rn(float x, float y) { return __fmul_rn(x, y); }
+__device__ __forceinline__ double mul_rn(double x, double y) { return __dmul_rn(x, y); }
+
+template <typename T>
+__device__ __forceinline__ void chain_next(T av, T bv, T cv, T z, T& xnext, T xlast) {
+    xnext = mul_rn(av, fma(-cv, xlast, fma(-bv, xnext, z)));
+}
+
+// a, b, c point at mode j's first coefficient (global or shared memory); bead p's is p * ld
+// further (ld = N: the table is bead-major, so the threads of a tile that run different modes read
+// neighbouring words)
 template <typename T>
 __device__ __forceinline__ void chain_step(const T* __restrict__ a, const T* __restrict__ b,
-                                           const T* __restrict__ c, int p, int P, T z, T& xnext, T& xlast) {
-    T x;
+                                           const T* __restrict__ c, int p, int P, int ld, T z, T& xnext,
+                                           T& xlast) {
+    const int o = p * ld;
     if (p == P - 1) {
-        x = __ldg(a + p) * z;
-        xlast = x;
+        xnext = mul_rn(a[o], z);
+        xlast = xnext;
     } else {
-        const T u = fma(-__ldg(b + p), xnext, z);
-        x = __ldg(a + p) * fma(-__ldg(c + p), xlast, u);
+        chain_next<T>(a[o], b[o], c[o], z, xnext, xlast);
     }
-    xnext = x;
 }
 
 template <typename T, typename Sink>
 __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, uint64_t sg, uint32_t key0,
                                                    uint32_t key1, T dsh, Sink&& sink) {
     const int N = m.N, P = m.P;
-    const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
+    const T* a = static_cast<const T*>(m.ring_chol) + j;
     const T* b = a + static_cast<int64_t>(N) * P;
     const T* c = b + static_cast<int64_t>(N) * P;
     const uint32_t lo = static_cast<uint32_t>(sg), hi = static_cast<uint32_t>(sg >> 32);
@@ -368,7 +405,7 @@ __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, ui
         for (int t = 3; t >= 0; --t) {
             const int p = 4 * p4 + t;
             if (p >= P) continue;
-            chain_step<T>(a, b, c, p, P, T(z[t]), xnext, xlast);
+            chain_step<T>(a, b, c, p, P, N, T(z[t]), xnext, xlast);
             sink(p, xnext + dsh);
         }
     }
@@ -405,17 +442,56 @@ __device__ __forceinline__ void fill_normals(const pbr_model& m, T* qs, int qstr
     }
 }
 
-// mode j of one sample, in place: normals in, q = x + dsh out (qj = the mode's row, skewed layout)
-template <typename T>
-__device__ __forceinline__ void back_substitute(const pbr_model& m, int j, T dsh, T* qj) {
-    const int N = m.N, P = m.P;
-    const T* a = static_cast<const T*>(m.ring_chol) + static_cast<int64_t>(j) * P;
+// mode j of one sample, in place: normals in, q = x + dsh out (qj = the mode's row, skewed layout;
+// tab = the ring factor [3][P][N], in global or shared memory).  The chain is serial, so the
+// coefficients and normals of the next kBsGroup steps are loaded while the current group runs;
+// the arithmetic is chain_step's.
+constexpr int kBsGroup = 4;
+template <typename T, int W = kBsGroup>
+__device__ __forceinline__ void back_substitute(const T* tab, int N, int P, int j, T dsh, T* qj) {
+    const T* a = tab + j;
     const T* b = a + static_cast<int64_t>(N) * P;
     const T* c = b + static_cast<int64_t>(N) * P;
     T xnext = T(0), xlast = T(0);
-    for (int p = P - 1; p >= 0; --p) {
+    {
+        T* slot = qj + (P - 1) + ((P - 1) >> 5);
+        chain_step<T>(a, b, c, P - 1, P, N, *slot, xnext, xlast);
+        *slot = xnext + dsh;
+    }
+    int p = P - 2;
+    if (p >= W - 1) {
+        T ca[W], cb[W], cc[W], cz[W];
+#pragma unroll
+        for (int t = 0; t < W; ++t) {
+            const int q = p - t;
+            ca[t] = a[q * N]; cb[t] = b[q * N]; cc[t] = c[q * N]; cz[t] = qj[q + (q >> 5)];
+        }
+        while (true) {
+            const int pn = p - W;
+            const bool more = pn >= W - 1;
+            T na[W], nb[W], nc[W], nz[W];
+            if (more) {
+#pragma unroll
+                for (int t = 0; t < W; ++t) {
+                    const int q = pn - t;
+                    na[t] = a[q * N]; nb[t] = b[q * N]; nc[t] = c[q * N]; nz[t] = qj[q + (q >> 5)];
+                }
+            }
+#pragma unroll
+            for (int t = 0; t < W; ++t) {
+                const int q = p - t;
+                chain_next<T>(ca[t], cb[t], cc[t], cz[t], xnext, xlast);
+                qj[q + (q >> 5)] = xnext + dsh;
+            }
+            p = pn;
+            if (!more) break;
+#pragma unroll
+            for (int t = 0; t < W; ++t) { ca[t] = na[t]; cb[t] = nb[t]; cc[t] = nc[t]; cz[t] = nz[t]; }
+        }
+    }
+    for (; p >= 0; --p) {
         T* slot = qj + p + (p >> 5);
-        chain_step<T>(a, b, c, p, P, *slot, xnext, xlast);
+        chain_step<T>(a, b, c, p, P, N, *slot, xnext, xlast);
         *slot = xnext + dsh;
     }
 }
@@ -431,7 +507,8 @@ __device__ int draw_sample_smem(const pbr_model& m, T* qs, int rs, int64_t sidx,
     const int src = draw_source<T>(m, sg, key0, key1);
     const T* dsrc = static_cast<const T*>(m.rho_d) + static_cast<int64_t>(src) * N;
     __syncwarp(gmask);
-    for (int j = g; j < N; j += G) back_substitute<T>(m, j, dsrc[j], qs + j * rs);
+    for (int j = g; j < N; j += G)
+        back_substitute<T>(static_cast<const T*>(m.ring_chol), N, m.P, j, dsrc[j], qs + j * rs);
     __syncwarp(gmask);
     return src;
 }
@@ -682,12 +759,10 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                 //      previous bead) in the FP64 validation build ----
                 T M[A][A];
                 if constexpr (sizeof(T) == 4 && A >= kExpmMinA) {
-                    T am[A][A];
+                    float vp[npair(A)];
 #pragma unroll
-                    for (int b = 0; b < A; ++b)
-#pragma unroll
-                        for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
-                    nexp += expm_neg_tau<A>(am, static_cast<float>(m.tau), M);
+                    for (int i = 0; i < npair(A); ++i) vp[i] = v[i];
+                    nexp += expm_neg_tau<A>(vp, static_cast<float>(m.tau), M);
                 } else {
                     const bool cold = ((p - p_begin) & 7) == 0;   // fresh basis every 8 beads
                     if (cold) {

@@ -23,7 +23,7 @@ namespace pbr {
 constexpr int kTeamThreads = 256;
 // largest surface count whose exp(-tau V) is formed by scaling and squaring in one thread's
 // registers (FP32); beyond it the per-thread Jacobi of the FP64 form is used
-constexpr int kTeamExpmMaxA = 6;
+constexpr int kTeamExpmMaxA = 8;
 
 struct TeamArgs {
     pbr_model m;
@@ -53,8 +53,10 @@ __host__ __device__ inline int record_len(int A, int K) { return align_up(A * A 
 
 struct TeamPlan {
     int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
+    int alt;          // second buffer of combine slots (the split combine), or -1: none fits
+    bool stage_ring;  // the ring factor fits the bead-record region (phase A copies it there)
     __host__ __device__ TeamPlan() : c(0), e(0), qq(0), rc(0), rec(0), src(0), q(0), qlo(0), beads(0),
-                                     lsums(0), total_bytes(0) {}
+                                     lsums(0), total_bytes(0), alt(-1), stage_ring(false) {}
     __host__ __device__ TeamPlan(int A, int K, int qm, int esz, int N, int P, int S, int G, int qstride,
                                  int rl) {
         const int A2P = align_up(npair(A), 4);
@@ -69,6 +71,10 @@ struct TeamPlan {
         int nb = S * P * rl;
         nb = nb > comb ? nb : comb;
         beads = take(nb);
+        // the split combine's second slot buffer: the rest of the bead-record region, else the q
+        // tile (both are free once B1 is done)
+        alt = (nb >= 2 * comb) ? beads + comb : (S * qstride >= comb ? q : -1);
+        stage_ring = 3 * N * P <= nb && (beads * esz) % 16 == 0;
         lsums = take((S * G * (A + 2) * 8 + esz - 1) / esz);      // 8-byte log sums + exponent slot
         total_bytes = o * esz;
     }
@@ -118,8 +124,11 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
 }
 
 // One tile of S samples starting at global sample `base` (phases A, B1, B2, C, D); ends with a
-// block barrier, so the caller may reload the tables afterwards.
-template <int A, int K, int QM, typename T>
+// block barrier, so the caller may reload the tables afterwards.  MB is the blocks per SM the
+// build targets; the two-block build (128 registers) uses the forms that need fewer registers:
+// the receiver combine, a two-step prefetch in the chains and, at 5 surfaces, a B2 that streams
+// the bead matrices column by column (at 6 surfaces that form measured slower than its spills).
+template <int A, int K, int QM, typename T, int MB = 1>
 __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int64_t base) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
@@ -130,6 +139,8 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     constexpr int OFF_O = A * A, OFF_L = A * A + (K + 1) * A, OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
     constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
     constexpr int NT = kTeamThreads;
+    constexpr bool kTwoBlock = MB > 1;
+    constexpr bool kLeanB2 = kTwoBlock && A == 5;
 
     const pbr_model& m = args.m;
     const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
@@ -160,17 +171,33 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
 
         // ================================ phase A ==============================================
         if (QM == kSample) {
+            // The ring factor [3][P][N] is copied asynchronously into the bead-record region (free
+            // until B1) when it fits: the chains below then read shared memory, not L2.
+            const T* tab = static_cast<const T*>(m.ring_chol);
+            const bool stage = plan.stage_ring && (reinterpret_cast<uintptr_t>(tab) & 15) == 0;
+            if (stage) {
+                const int nbytes = 3 * N * P * static_cast<int>(sizeof(T));
+                const char* gsrc = reinterpret_cast<const char*>(tab);
+                const uint32_t sdst = static_cast<uint32_t>(__cvta_generic_to_shared(s_beads));
+                for (int o = 16 * tid; o + 16 <= nbytes; o += 16 * NT)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" :: "r"(sdst + o), "l"(gsrc + o) : "memory");
+                for (int o = (nbytes & ~15) + 4 * tid; o < nbytes; o += 4 * NT)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(sdst + o), "l"(gsrc + o) : "memory");
+                asm volatile("cp.async.commit_group;" ::: "memory");
+                tab = s_beads;
+            }
             for (int s = tid; s < S; s += NT)
                 s_src[s] = (s < nvalid) ? draw_source<T>(m, args.offset + static_cast<uint64_t>(base + s),
                                                          args.key0, args.key1) : 0;
             // the tile's normals over all threads, then one back-substitution chain per (sample, mode)
             fill_normals<T>(m, s_q, args.qstride, rs, nvalid, args.offset + static_cast<uint64_t>(base),
                             args.key0, args.key1, tid, NT);
+            if (stage) asm volatile("cp.async.wait_all;" ::: "memory");
             __syncthreads();
             for (int it = tid; it < nvalid * N; it += NT) {
                 const int s = it / N, j = it - s * N;
                 const T dsh = static_cast<const T*>(m.rho_d)[static_cast<int64_t>(s_src[s]) * N + j];
-                back_substitute<T>(m, j, dsh, s_q + s * args.qstride + j * rs);
+                back_substitute<T, kTwoBlock ? 2 : kBsGroup>(tab, N, P, j, dsh, s_q + s * args.qstride + j * rs);
             }
             __syncthreads();
             if (args.out.q_out) {
@@ -334,16 +361,14 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
             }
             if constexpr (sizeof(T) == 4 && A >= kExpmMinA && A <= kTeamExpmMaxA) {
                 // M = exp(-tau V) by scaling and squaring in registers (see expm_neg_tau)
-                T am[A][A], Mx[A][A];
+                float vp[A2], X[A2], f;
+#pragma unroll
+                for (int i = 0; i < A2; ++i) vp[i] = v[i];
+                rec_out[OFF_N] = T(expm_neg_tau_packed<A>(vp, static_cast<float>(m.tau), X, f));
 #pragma unroll
                 for (int b = 0; b < A; ++b)
 #pragma unroll
-                    for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
-                rec_out[OFF_N] = T(expm_neg_tau<A>(am, static_cast<float>(m.tau), Mx));
-#pragma unroll
-                for (int b = 0; b < A; ++b)
-#pragma unroll
-                    for (int c = 0; c < A; ++c) rec_out[b * A + c] = Mx[b][c];
+                    for (int c = 0; c < A; ++c) rec_out[b * A + c] = f * X[sym_index(b, c)];
             } else {
                 T am[A][A], u[A][A];
 #pragma unroll
@@ -395,7 +420,47 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                 nexp += static_cast<int>(rc_[OFF_N]);
                 if (r == 0) ls.add(rc_[OFF_L]);
                 if (r < A && r < nfill) lr.add(rc_[OFF_R + (r < A ? r : 0)]);
-                if (r < A) {
+                if (r < A && kLeanB2) {
+                    // column c of N M diag(O(c)): y = N(:, .) M(., c), then the series convolution
+                    T nn[K + 1][A];
+#pragma unroll
+                    for (int c = 0; c < A; ++c) {
+                        T mc[A], oc[K + 1];
+#pragma unroll
+                        for (int mm = 0; mm < A; ++mm) mc[mm] = rc_[mm * A + c];
+#pragma unroll
+                        for (int k = 0; k <= K; ++k) oc[k] = rc_[OFF_O + k * A + c];
+                        if (p == pb) {
+#pragma unroll
+                            for (int k = 0; k <= K; ++k) {
+                                T mrc = T(0);
+#pragma unroll
+                                for (int b = 0; b < A; ++b) mrc = (b == r) ? mc[b] : mrc;
+                                nn[k][c] = mrc * oc[k];
+                            }
+                        } else {
+                            T yc[K + 1];
+#pragma unroll
+                            for (int i = 0; i <= K; ++i) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int mm = 0; mm < A; ++mm) acc = fma(nrow[i][mm], mc[mm], acc);
+                                yc[i] = acc;
+                            }
+#pragma unroll
+                            for (int k = 0; k <= K; ++k) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int i = 0; i <= k; ++i) acc = fma(yc[i], oc[k - i], acc);
+                                nn[k][c] = acc;
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) nrow[k][c] = nn[k][c];
+                } else if (r < A) {
                     T mf[A * A], of[(K + 1) * A];
                     ldv(rc_, mf);
                     ldv(rc_ + OFF_O, of);
@@ -472,63 +537,23 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
         __syncthreads();     // every thread is done reading bead records: the combine slots reuse them
 
         // ================================ phase C: combine chunks ==============================
-        T* comb = s_beads;
-        int* cexp = reinterpret_cast<int*>(s_lsum + S * G * (A + 1));
-        const int slot = ts * G + tc;
-        if (tact) {
-            if (r < A)
-#pragma unroll
-                for (int k = 0; k <= K; ++k)
-#pragma unroll
-                    for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
-            if (r < A) s_lsum[slot * (A + 1) + r] = lr;
-            if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
-        }
-        __syncthreads();
-        for (int st = 1; st < G; st <<= 1) {
-            const bool recv = tact && (tc % (2 * st)) == 0 && tc + st < G;
-            if (recv) {
-                const int ps = slot + st;
-                const T* Y = comb + ps * CL;
-                if (r < A) {
-                    T z[K + 1][A];
-#pragma unroll
-                    for (int k = 0; k <= K; ++k)
-#pragma unroll
-                        for (int c = 0; c < A; ++c) {
-                            T acc = T(0);
-#pragma unroll
-                            for (int i = 0; i <= k; ++i)
-#pragma unroll
-                                for (int mm = 0; mm < A; ++mm) acc = fma(nrow[i][mm], Y[((k - i) * A + mm) * A + c], acc);
-                            z[k][c] = acc;
-                        }
-#pragma unroll
-                    for (int k = 0; k <= K; ++k)
-#pragma unroll
-                        for (int c = 0; c < A; ++c) nrow[k][c] = z[k][c];
-                    lr.merge(s_lsum[ps * (A + 1) + r]);
-                }
-                if (r == 0) ls.merge(s_lsum[ps * (A + 1) + A]);
-                nexp += cexp[ps];
-                T mx = T(0);
-                if (r < A) {
-#pragma unroll
-                    for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nrow[0][c]));
-                }
-#pragma unroll
-                for (int o = TA / 2; o >= 1; o >>= 1) mx = max(mx, __shfl_xor_sync(tmask, mx, o, TA));
-                if (mx > T(0) && isfinite(mx)) {
-                    int e2;
-                    frexp(mx, &e2);
-                    const T sc = ldexp(T(1), -e2);
-                    nexp += e2;
-#pragma unroll
-                    for (int k = 0; k <= K; ++k)
-#pragma unroll
-                        for (int c = 0; c < A; ++c) nrow[k][c] *= sc;
-                }
-                // own slot is no other receiver's partner at this level: write it back now
+        // Level st multiplies the chunk pairs (t0, t0 + st), t0 a multiple of 2 st, in bead order.
+        // Split form (a second slot buffer fits and registers allow): all 2 st teams of the pair's
+        // range work on its product, team u taking column group u of min(2 st, A) balanced groups,
+        // thread r row r; products alternate between the two slot buffers (one barrier per level)
+        // and the log sums and exponents merge in place (a pair's scalars are touched by one
+        // thread).  The chunks enter normalised (max |N_0| in [1/2, 1)) and their products are not
+        // renormalised: log2 G <= 5 levels move the entries by far less than the FP32 range, and
+        // power-of-two scaling would not change a rounding.  Receiver form (the two-block build, or
+        // no room): the team of chunk t0 multiplies its rows, held in registers, by its partner's
+        // slot and renormalises.
+        if (!kTwoBlock && plan.alt >= 0) {
+            constexpr int CW = (A + 1) / 2;                        // most columns of one team
+            T* comb = s_beads;
+            T* comb_alt = sm + plan.alt;
+            int* cexp = reinterpret_cast<int*>(s_lsum + S * G * (A + 1));
+            const int slot = ts * G + tc;
+            if (tact) {
                 if (r < A)
 #pragma unroll
                     for (int k = 0; k <= K; ++k)
@@ -538,6 +563,133 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                 if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
             }
             __syncthreads();
+            for (int st = 1; st < G; st <<= 1) {
+                const int t0 = tc & ~(2 * st - 1), u = tc - t0;
+                const int xs = ts * G + t0, ys = xs + st;
+                const int ngrp = min(2 * st, A);
+                if (tact && r < A && u < ngrp) {
+                    const int c0 = (u * A) / ngrp, nc = ((u + 1) * A) / ngrp - c0;
+                    const T* X = comb + xs * CL;
+                    const T* Y = comb + ys * CL;
+                    T* Z = comb_alt + xs * CL;
+                    T xr[K + 1][A];
+#pragma unroll
+                    for (int i = 0; i <= K; ++i)
+#pragma unroll
+                        for (int mm = 0; mm < A; ++mm) xr[i][mm] = X[(i * A + r) * A + mm];
+#pragma unroll
+                    for (int cc = 0; cc < CW; ++cc) {
+                        if (cc < nc) {
+                            const int c = c0 + cc;
+#pragma unroll
+                            for (int k = 0; k <= K; ++k) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int i = 0; i <= k; ++i)
+#pragma unroll
+                                    for (int mm = 0; mm < A; ++mm) acc = fma(xr[i][mm], Y[((k - i) * A + mm) * A + c], acc);
+                                Z[(k * A + r) * A + c] = acc;
+                            }
+                        }
+                    }
+                }
+                if (tact && u == 0) {
+                    if (r < A) {
+                        LogSum<T> x = s_lsum[xs * (A + 1) + r];
+                        x.merge(s_lsum[ys * (A + 1) + r]);
+                        s_lsum[xs * (A + 1) + r] = x;
+                    }
+                    if (r == 0) {
+                        LogSum<T> x = s_lsum[xs * (A + 1) + A];
+                        x.merge(s_lsum[ys * (A + 1) + A]);
+                        s_lsum[xs * (A + 1) + A] = x;
+                        cexp[xs] += cexp[ys];
+                    }
+                }
+                __syncthreads();
+                T* sw = comb; comb = comb_alt; comb_alt = sw;
+            }
+            // the sample's product, log sums and exponent for phase D's team (tc == 0)
+            if (tact && tc == 0 && G > 1) {
+                const int s0 = ts * G;
+                if (r < A) {
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) nrow[k][c] = comb[s0 * CL + (k * A + r) * A + c];
+                    lr = s_lsum[s0 * (A + 1) + r];
+                }
+                if (r == 0) ls = s_lsum[s0 * (A + 1) + A];
+                nexp = cexp[s0];
+            }
+        } else {
+            T* comb = s_beads;
+            int* cexp = reinterpret_cast<int*>(s_lsum + S * G * (A + 1));
+            const int slot = ts * G + tc;
+            if (tact) {
+                if (r < A)
+#pragma unroll
+                    for (int k = 0; k <= K; ++k)
+#pragma unroll
+                        for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
+                if (r < A) s_lsum[slot * (A + 1) + r] = lr;
+                if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
+            }
+            __syncthreads();
+            for (int st = 1; st < G; st <<= 1) {
+                const bool recv = tact && (tc % (2 * st)) == 0 && tc + st < G;
+                if (recv) {
+                    const int ps = slot + st;
+                    const T* Y = comb + ps * CL;
+                    if (r < A) {
+                        T z[K + 1][A];
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) {
+                                T acc = T(0);
+#pragma unroll
+                                for (int i = 0; i <= k; ++i)
+#pragma unroll
+                                    for (int mm = 0; mm < A; ++mm) acc = fma(nrow[i][mm], Y[((k - i) * A + mm) * A + c], acc);
+                                z[k][c] = acc;
+                            }
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) nrow[k][c] = z[k][c];
+                        lr.merge(s_lsum[ps * (A + 1) + r]);
+                    }
+                    if (r == 0) ls.merge(s_lsum[ps * (A + 1) + A]);
+                    nexp += cexp[ps];
+                    T mx = T(0);
+                    if (r < A) {
+#pragma unroll
+                        for (int c = 0; c < A; ++c) mx = max(mx, dev_fabs(nrow[0][c]));
+                    }
+#pragma unroll
+                    for (int o = TA / 2; o >= 1; o >>= 1) mx = max(mx, __shfl_xor_sync(tmask, mx, o, TA));
+                    if (mx > T(0) && isfinite(mx)) {
+                        int e2;
+                        frexp(mx, &e2);
+                        const T sc = ldexp(T(1), -e2);
+                        nexp += e2;
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) nrow[k][c] *= sc;
+                    }
+                    // own slot is no other receiver's partner at this level: write it back now
+                    if (r < A)
+#pragma unroll
+                        for (int k = 0; k <= K; ++k)
+#pragma unroll
+                            for (int c = 0; c < A; ++c) comb[slot * CL + (k * A + r) * A + c] = nrow[k][c];
+                    if (r < A) s_lsum[slot * (A + 1) + r] = lr;
+                    if (r == 0) { s_lsum[slot * (A + 1) + A] = ls; cexp[slot] = nexp; }
+                }
+                __syncthreads();
+            }
         }
 
         // ================================ phase D: outputs =====================================
@@ -602,7 +754,7 @@ __global__ void __launch_bounds__(kTeamThreads, MB) pimc_team_kernel(const TeamA
     __syncthreads();
     for (int64_t base = static_cast<int64_t>(blockIdx.x) * args.S; base < args.X;
          base += static_cast<int64_t>(gridDim.x) * args.S)
-        team_tile<A, K, QM, T>(args, sm, plan, base);
+        team_tile<A, K, QM, T, MB>(args, sm, plan, base);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -637,7 +789,7 @@ pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int
             __syncthreads();
             cur = lo;
         }
-        team_tile<A, K, kSample, float>(a, sm, plan, (t - items[lo].tile_begin) * a.S);
+        team_tile<A, K, kSample, float, MB>(a, sm, plan, (t - items[lo].tile_begin) * a.S);
     }
 }
 

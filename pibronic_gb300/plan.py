@@ -219,7 +219,8 @@ class PreparedModels:
                             qq[row, pair_index(b, c)] = 0.5 * Q[d, d, b, c]
                         else:
                             qq[row, pair_index(b, c)] = 0.5 * (Q[d, e_, b, c] + Q[e_, d, b, c])
-        ring_chol = ring_precision_factor(self.rho_omega, self.tau, P)
+        # bead-major [3][P][N]: the threads that run different modes at one bead read neighbours
+        ring_chol = np.ascontiguousarray(ring_precision_factor(self.rho_omega, self.tau, P).transpose(0, 2, 1))
         return {
             "vib_cs": 0.5 * csch_s.T.copy(), "vib_th": 0.5 * tanh_s.T.copy(), "vib_c": vib_c.T.copy(),
             "vib_d": self.vib_shift.copy(), "vib_e": e, "vib_l": lt.reshape(N, A2), "vib_qq": qq,
