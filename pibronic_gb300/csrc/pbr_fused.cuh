@@ -397,6 +397,14 @@ __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, ui
     const int CP = (P + 3) >> 2;
     T xnext = T(0), xlast = T(0);
     for (int p4 = (P - 1) >> 2; p4 >= 0; --p4) {
+        // the group's coefficients are loaded first, so their latency hides behind Philox
+        T ka[4], kb[4], kc[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int p = 4 * p4 + t;
+            const int o = (p < P ? p : 0) * N;
+            ka[t] = a[o]; kb[t] = b[o]; kc[t] = c[o];
+        }
         const u32x4 r = philox4x32_10(u32x4{static_cast<uint32_t>(j * CP + p4), lo, hi, 0u}, key0, key1);
         float z[4];
         box_muller(r.x, r.y, z[0], z[1]);
@@ -405,7 +413,12 @@ __device__ __forceinline__ void draw_mode_chain_to(const pbr_model& m, int j, ui
         for (int t = 3; t >= 0; --t) {
             const int p = 4 * p4 + t;
             if (p >= P) continue;
-            chain_step<T>(a, b, c, p, P, N, T(z[t]), xnext, xlast);
+            if (p == P - 1) {
+                xnext = mul_rn(ka[t], T(z[t]));
+                xlast = xnext;
+            } else {
+                chain_next<T>(ka[t], kb[t], kc[t], T(z[t]), xnext, xlast);
+            }
             sink(p, xnext + dsh);
         }
     }
