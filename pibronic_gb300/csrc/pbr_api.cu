@@ -146,11 +146,12 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
     while (true) {
         a.S = kThreads / a.G;
-        const SmemPlan plan(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride);
-        if (plan.total_bytes <= kMaxSmem || a.G == 32) {
-            if (plan.total_bytes > kMaxSmem) return PBR_ERR_UNSUPPORTED;
-            break;
-        }
+        // the tensor-core quadratic where it applies and its tables fit, else the pair loop
+        const SmemPlan pt(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride, 1);
+        const SmemPlan p0(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride, 0);
+        if (pt.total_bytes <= kMaxSmem) { a.tcq = pt.tcq_k > 0 ? 1 : 0; break; }
+        if (p0.total_bytes <= kMaxSmem) { a.tcq = 0; break; }
+        if (a.G == 32) return PBR_ERR_UNSUPPORTED;
         a.G *= 2;
     }
     a.logG = ilog2(a.G);

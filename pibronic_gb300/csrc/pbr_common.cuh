@@ -9,6 +9,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/pibronic_gb300.h"
@@ -177,6 +178,21 @@ __device__ __forceinline__ void jacobi_eigh(T (&a)[A][A], T (&u)[A][A], int max_
 // ----------------------------------------------------------------------------------------------
 __device__ __forceinline__ void flag_status(int32_t* status, int32_t code) {
     if (status) atomicMax(status, code);
+}
+
+// FP16 pair (x0, x1), x0 in the low half
+__device__ __forceinline__ uint32_t pack_f16x2(float x0, float x1) {
+    uint32_t r;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(x1), "f"(x0));
+    return r;
+}
+
+// hi = FP16(x) and lo = FP16(x - hi) for two values, packed as FP16 pairs
+__device__ __forceinline__ void split_f16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    hi = pack_f16x2(x0, x1);
+    const __half2 h = *reinterpret_cast<const __half2*>(&hi);
+    const float2 hf = __half22float2(h);
+    lo = pack_f16x2(x0 - hf.x, x1 - hf.y);
 }
 
 }  // namespace pbr

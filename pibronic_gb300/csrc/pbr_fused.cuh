@@ -26,6 +26,12 @@
 namespace pbr {
 
 constexpr int kThreads = 128;
+// the tensor-core quadratic is used at 3-4 surfaces from this many modes on (measured: 8 % faster
+// at A = 4, N = 20; 1-6 % slower at N = 8-12, where the FP32 pair loop is short);
+// records whose |q| exceeds kTcqMaxQ keep every q_d q_e below 2^15, inside FP16's range -- a warp
+// holding a larger one takes the FP32 pair loop for that bead
+constexpr int kTcqMinN = 16;
+constexpr float kTcqMaxQ = 181.0f;
 // target beads per thread (chunk length) of the ring product: 16 rather than 8 halves the
 // threads per sample, so fewer chunk products to combine, fewer chains idle in the sampler's
 // second pass and the per-sample outputs spread over more beads (A = 4, N = 12, P = 64: 15.25 ->
@@ -45,6 +51,7 @@ struct FusedArgs {
     int G, logG, C, S;
     int rs;         // row stride of one mode's beads in shared memory (skewed, see qidx)
     int qstride;    // elements per sample in the q region
+    int tcq;        // 1: the tensor-core quadratic (its tables, its kernel instantiation)
 };
 
 __host__ __device__ inline int align_up(int x, int a) { return (x + a - 1) / a * a; }
@@ -62,13 +69,32 @@ __host__ __device__ inline int rec_len(int A, int K) {
 }
 
 // Shared-memory plan (in elements of the table type, esz bytes each); identical on host and device.
+// Tensor-core quadratic part of V in the register-chunk form (FP32 build, A <= 4): the mode
+// pairs (d, e <= d) are grouped in quadruples (d, e0 .. e0+3) -- one FP16 MMA k-step of 16 pair
+// slots holds four quadruples -- and the warp's 32 (sample, bead) records form the MMA's rows.
+__host__ __device__ inline int tcq_quads(int N) {
+    int n = 0;
+    for (int d = 0; d < N; ++d) n += (d + 4) / 4;        // ceil((d + 1) / 4) per row d
+    return n;
+}
+__host__ __device__ inline int tcq_ksteps(int N) { return (tcq_quads(N) + 3) / 4; }
+__host__ __device__ constexpr int tcq_ntiles(int A) { return (npair(A) + 7) / 8; }
+// 32-bit words: B fragments (k-steps x n-tiles x 32 lanes x 4), quadruple descriptors (int4 per
+// quadruple), the inverse coupling scale
+__host__ __device__ inline int tcq_words(int N, int A) {
+    return tcq_ksteps(N) * tcq_ntiles(A) * 128 + tcq_ksteps(N) * 16 + 4;
+}
+
 struct SmemPlan {
     int c, e, qq, rc, rec, q, qlo, total_bytes;
-    __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int S, int qstride) {
+    int tcq_k;   // k-steps of the tensor-core quadratic (0: the FP32 pair loop over a packed table)
+    __host__ __device__ SmemPlan(int A, int K, int qm, int esz, int N, int P, int S, int qstride, int tcq) {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        c = take((K + 1) * A); e = take(A2P); qq = take(npair(N) * A2P); rc = take(A);
+        // the quadruple descriptors hold mode offsets d * rs in 16 bits
+        tcq_k = (tcq && esz == 4 && A >= 3 && A <= 4 && N >= kTcqMinN && qstride - 1 < 65536) ? tcq_ksteps(N) : 0;
+        c = take((K + 1) * A); e = take(A2P); qq = take(tcq_k ? tcq_words(N, A) : npair(N) * A2P); rc = take(A);
         rec = take(N * rec_len(A, K));
         q = take(S * qstride);
         qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
@@ -547,7 +573,153 @@ __device__ __forceinline__ int renormalise(T (&n)[K + 1][A][A]) {
     return e2;
 }
 
-template <int A, int K, int QM, typename T>
+// Shared-memory tables of the tensor-core quadratic, built by the whole block (ends with a
+// barrier): the couplings Q[pair][bc] scaled by 2^s (max |Q| 2^s in [2^13, 2^14), so their FP16
+// low parts stay normal), split into FP16 hi and lo and laid out as each lane's B fragment of
+// mma.m16n8k16 (rows 2t, 2t+1 = slots 0, 1 and rows 2t+8, 2t+9 = slots 2, 3 of quadruple 4 kk + t,
+// column g = surface pair 8 nt + g); per quadruple the offsets d rs and min(e0 + s, d) rs of its
+// four slots; then 2^-s.
+template <int A>
+__device__ void tcq_tables(const float* __restrict__ g_qq, int N, int rs, int nks, uint32_t* tq) {
+    constexpr int A2 = npair(A);
+    constexpr int NT = tcq_ntiles(A);
+    const int nq4 = 4 * nks;
+    int4* desc = reinterpret_cast<int4*>(tq + nks * NT * 128);
+    float* sinv = reinterpret_cast<float*>(desc + nq4);
+    if (threadIdx.x == 0) *reinterpret_cast<int*>(sinv) = 0;
+    __syncthreads();
+    float mx = 0.f;
+    for (int i = threadIdx.x; i < npair(N) * A2; i += blockDim.x) mx = fmaxf(mx, fabsf(g_qq[i]));
+    atomicMax(reinterpret_cast<int*>(sinv), __float_as_int(mx));       // non-negative floats order as ints
+    for (int u = threadIdx.x; u < nq4; u += blockDim.x) {
+        int4 r = make_int4(0, 0, 0, -1);                                  // padding: zero couplings
+        int base = 0;
+        for (int d = 0; d < N; ++d) {
+            const int nq = (d + 4) / 4;
+            if (u < base + nq) {
+                const int e0 = 4 * (u - base);
+                int o[4];
+#pragma unroll
+                for (int s = 0; s < 4; ++s) o[s] = min(e0 + s, d) * rs;
+                r = make_int4(static_cast<int>(static_cast<uint32_t>(d * rs) | (static_cast<uint32_t>(o[0]) << 16)),
+                              static_cast<int>(static_cast<uint32_t>(o[1]) | (static_cast<uint32_t>(o[2]) << 16)), o[3],
+                              (d << 16) | e0);
+                break;
+            }
+            base += nq;
+        }
+        desc[u] = r;
+    }
+    __syncthreads();
+    const float qmax = *sinv;
+    int e2 = 0;
+    if (qmax > 0.f) frexpf(qmax, &e2);
+    const int sq = (qmax > 0.f) ? 14 - e2 : 0;
+    const float sc = ldexpf(1.f, sq);
+    for (int i = threadIdx.x; i < nks * NT * 32; i += blockDim.x) {
+        const int lane = i & 31, tile = i >> 5, nt = tile % NT, kk = tile / NT;
+        const int bc = 8 * nt + (lane >> 2);
+        const int4 dsc = desc[4 * kk + (lane & 3)];
+        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        if (dsc.w >= 0 && bc < A2) {
+            const int d = dsc.w >> 16, e0 = dsc.w & 0xffff;
+#pragma unroll
+            for (int s = 0; s < 4; ++s)
+                if (e0 + s <= d) v[s] = g_qq[pair_index(d, e0 + s) * A2 + bc] * sc;
+        }
+        uint32_t h01, l01, h23, l23;
+        split_f16x2(v[0], v[1], h01, l01);
+        split_f16x2(v[2], v[3], h23, l23);
+        *reinterpret_cast<uint4*>(tq + 4 * i) = make_uint4(h01, h23, l01, l23);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *sinv = ldexpf(1.f, -sq);
+    __syncthreads();
+}
+
+// D (16 x 8, FP32) += A (16 x 16) B (16 x 8), FP16 operands
+__device__ __forceinline__ void mma_f16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// The quadratic part of V for the warp's 32 records, by the tensor cores: records are the MMA
+// rows (m-tile mt, row g / g + 8 = the record of lane 16 mt + g / 16 mt + 8 + g; a lane's
+// fragment rows are g = lane / 4 and g + 8), the pair slots
+// of four quadruples one k-step, the surface pairs the columns.  Each lane forms the products
+// q_d q_e of its four rows' records from shared memory (rec[r] = record 2 mt + half's q at its
+// bead, mode 0), split into FP16 hi and lo; three MMAs per tile (hi hi, hi lo, lo hi) give about
+// 22 bits.  Returns, in vq, this lane's own record's quadratic terms (already unscaled).
+template <int A>
+__device__ __forceinline__ void tcq_quadratic(const uint32_t* __restrict__ tq, int nks, const float* __restrict__ sq,
+                                              const int (&rec)[4], int lane, float (&vq)[npair(A)]) {
+    constexpr int A2 = npair(A);
+    constexpr int NT = tcq_ntiles(A);
+    const int4* desc = reinterpret_cast<const int4*>(tq + nks * NT * 128);
+    const float sinv = *reinterpret_cast<const float*>(desc + 4 * nks);
+    float acc[2][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[mt][nt][i] = 0.f;
+    for (int kk = 0; kk < nks; ++kk) {
+        const int4 dsc = desc[4 * kk + (lane & 3)];
+        const uint32_t ux = static_cast<uint32_t>(dsc.x), uy = static_cast<uint32_t>(dsc.y);
+        const int od = ux & 0xffffu, o0 = ux >> 16, o1 = uy & 0xffffu, o2 = uy >> 16, o3 = dsc.z;
+        uint32_t ah[2][4], al[2][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const float* qb = sq + rec[r];
+            const float qd = qb[od];
+            uint32_t h01, l01, h23, l23;
+            split_f16x2(qd * qb[o0], qd * qb[o1], h01, l01);
+            split_f16x2(qd * qb[o2], qd * qb[o3], h23, l23);
+            const int mt = r >> 1, hf = r & 1;
+            ah[mt][hf] = h01; ah[mt][2 + hf] = h23;
+            al[mt][hf] = l01; al[mt][2 + hf] = l23;
+        }
+        uint4 b[NT];
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) b[nt] = *reinterpret_cast<const uint4*>(tq + 4 * ((kk * NT + nt) * 32 + lane));
+        // the three passes outermost, so consecutive MMAs update different tiles
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass)
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+                for (int mt = 0; mt < 2; ++mt) {
+                    if (pass == 0) mma_f16_16816(acc[mt][nt], ah[mt], b[nt].x, b[nt].y);
+                    else if (pass == 1) mma_f16_16816(acc[mt][nt], ah[mt], b[nt].z, b[nt].w);
+                    else mma_f16_16816(acc[mt][nt], al[mt], b[nt].x, b[nt].y);
+                }
+    }
+    // D[row][col] of tile (mt, nt) sits in lane 4 (row % 8) + col % 8 / 2, register 2 (row / 8) +
+    // col % 2: this lane's record (mt = lane / 16, row half = lane / 8 % 2, row = lane % 8) reads
+    // its columns from the four lanes 4 (lane % 8) + t
+    const int pick = lane >> 3, src = 4 * (lane & 7);
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int tp = 0; tp < 4; ++tp)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int bc = 8 * nt + 2 * tp + e;
+                if (bc >= A2) continue;
+                const float s0 = __shfl_sync(0xffffffffu, acc[0][nt][e], src + tp);
+                const float s1 = __shfl_sync(0xffffffffu, acc[0][nt][2 + e], src + tp);
+                const float s2 = __shfl_sync(0xffffffffu, acc[1][nt][e], src + tp);
+                const float s3 = __shfl_sync(0xffffffffu, acc[1][nt][2 + e], src + tp);
+                vq[bc] = sinv * (pick == 0 ? s0 : pick == 1 ? s1 : pick == 2 ? s2 : s3);
+            }
+}
+
+// kTcq: the instantiation with the tensor-core quadratic (launched when args.tcq is set); the
+// other keeps the FP32 pair loop and none of the quadratic's registers.
+template <int A, int K, int QM, typename T, bool kTcq = false>
 __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs args) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
@@ -561,7 +733,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
     const pbr_model& m = args.m;
     const int N = m.N, P = m.P, nfill = m.n_fill_rho, rs = args.rs;
     const int G = args.G, C = args.C, S = args.S;
-    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, args.qstride);
+    const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), N, P, S, args.qstride, kTcq ? 1 : 0);
     T* s_c = sm + plan.c;    T* s_e = sm + plan.e;    T* s_qq = sm + plan.qq;
     T* s_rc = sm + plan.rc;  T* s_rec = sm + plan.rec;
 
@@ -576,9 +748,14 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
         for (int i = threadIdx.x; i < (K + 1) * A; i += blockDim.x) s_c[i] = g_c[i];
         for (int i = threadIdx.x; i < A2P; i += blockDim.x) s_e[i] = (i < A2) ? g_e[i] : T(0);
         const int N2 = npair(N);
-        for (int i = threadIdx.x; i < N2 * A2P; i += blockDim.x) {
-            const int row = i / A2P, col = i - row * A2P;
-            s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
+        if constexpr (kTcq) {
+            tcq_tables<A>(reinterpret_cast<const float*>(g_qq), N, rs, plan.tcq_k,
+                          reinterpret_cast<uint32_t*>(s_qq));
+        } else {
+            for (int i = threadIdx.x; i < N2 * A2P; i += blockDim.x) {
+                const int row = i / A2P, col = i - row * A2P;
+                s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
+            }
         }
         for (int i = threadIdx.x; i < A; i += blockDim.x) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
         for (int i = threadIdx.x; i < N * MR; i += blockDim.x) {
@@ -659,12 +836,20 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
         LogSum<T> lsum;
         T uw[A][A];          // eigenvectors of the previous bead: warm start of the next Jacobi
 
-        if (active) {
-            for (int p = p_begin; p < p_end; ++p) {
+        // One bead step of the chunk: bead p of the chunk (step ii), on = this lane's record is
+        // live.  Run by every lane for ii < C (the warp-wide tensor-core quadratic needs all 32
+        // records in step) in the tensor-core instantiation, and at 3 surfaces, where the uniform
+        // loop measured 17 % faster (A = 3, N = 8, P = 48); else only by live lanes over their own
+        // beads.
+        auto bead = [&](const int ii, const int p, const bool on) {
+            const int ip = qidx(0, p, rs);
+            T v[A2P], osr[K + 1][A];
+            T qmax = T(0);
+            if (on) {
                 const int pn = (p + 1 == P) ? 0 : p + 1;
-                const int ip = qidx(0, p, rs), ipn = qidx(0, pn, rs);
+                const int ipn = qidx(0, pn, rs);
                 // ---- O-matrix exponents and the linear part of V, one pass over the modes ----
-                T phv[K + 1][A], phr[A], v[A2P];
+                T phv[K + 1][A], phr[A];
 #pragma unroll
                 for (int k = 0; k <= K; ++k)
 #pragma unroll
@@ -686,6 +871,7 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                     ldv(rec + 2 * KP + 2 * AP, rx);
                     ldv(rec + 2 * KP + 2 * AP + 4, lr);
                     const T qa = qs[ip + j * rs], qb = qs[ipn + j * rs];
+                    if constexpr (kTcq) qmax = max(qmax, dev_fabs(qa));
                     T dq = qa - qb;
                     if (kLo) dq += ql[ip + j * rs] - ql[ipn + j * rs];
                     const T dq2 = dq * dq;
@@ -723,7 +909,6 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                 for (int a = 0; a < A; ++a)
                     if (a < nfill) lrho[a].add(phr[a] - lmax);
-                T osr[K + 1][A];
 #pragma unroll
                 for (int a = 0; a < A; ++a) {
                     T ek[K + 1];
@@ -739,8 +924,46 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
 #pragma unroll
                     for (int k = 0; k <= K; ++k) osr[k][a] = e0 * ek[k];
                 }
-                // ---- quadratic part of V: one flat loop over the mode pairs (d, e <= d) in table
-                //      order, unrolled so several pairs' loads are in flight together ----
+            }
+            // ---- quadratic part of V ----
+            bool quad_done = false;
+            if constexpr (kTcq) {
+                {
+                    // tensor cores, unless a record of the warp has a coordinate beyond FP16's
+                    // range for the products (then the FP32 loop below over the global table)
+                    if (!__any_sync(0xffffffffu, on && !(qmax <= T(kTcqMaxQ)))) {
+                        int rec[4];
+                        const int wb = tid & ~31;
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            const int l2 = wb + 16 * (r >> 1) + 8 * (r & 1) + (lane >> 2);   // fragment rows: lane / 4 (+ 8)
+                            const int pb = min((l2 & (G - 1)) * C + ii, P - 1);
+                            rec[r] = plan.q + (l2 >> args.logG) * args.qstride + qidx(0, pb, rs);
+                        }
+                        float vq[A2];
+                        tcq_quadratic<A>(reinterpret_cast<const uint32_t*>(s_qq), plan.tcq_k,
+                                         reinterpret_cast<const float*>(sm), rec, lane, vq);
+#pragma unroll
+                        for (int pr = 0; pr < A2; ++pr) v[pr] += vq[pr];
+                    } else if (on) {
+                        const float* gq = static_cast<const float*>(m.vib_qq);
+                        const int N2 = npair(N);
+                        int od = 0, oe = 0;
+                        for (int row = 0; row < N2; ++row) {
+                            const T w = qs[ip + od] * qs[ip + oe];
+#pragma unroll
+                            for (int pr = 0; pr < A2; ++pr) v[pr] = fma(__ldg(gq + row * A2 + pr), w, v[pr]);
+                            const bool wrap = (oe == od);
+                            od = wrap ? od + rs : od;
+                            oe = wrap ? 0 : oe + rs;
+                        }
+                    }
+                    quad_done = true;
+                }
+            }
+            if (on && !quad_done) {
+                // one flat loop over the mode pairs (d, e <= d) in table order, unrolled so
+                // several pairs' loads are in flight together
                 if constexpr (A >= kFlatPairsMinA) {
                     const int N2 = npair(N);
                     int od = 0, oe = 0;                  // offsets d * rs, e * rs of the pair (d, e)
@@ -768,6 +991,8 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                         }
                     }
                 }
+            }
+            if (on) {
                 // ---- M = exp(-tau V): scaling and squaring in FP32, Jacobi (warm-started from the
                 //      previous bead) in the FP64 validation build ----
                 T M[A][A];
@@ -867,6 +1092,13 @@ __global__ void __launch_bounds__(kThreads) pimc_fused_kernel(const FusedArgs ar
                 }
                 nexp += renormalise<T, K, A>(nser);
             }
+        };
+        if constexpr (kTcq || A == 3) {
+            if constexpr (kTcq) __syncwarp();  // the quadratic reads the q of every sample of the warp
+            for (int ii = 0; ii < C; ++ii) bead(ii, p_begin + ii, active && p_begin + ii < p_end);
+        } else {
+            if (active)
+                for (int p = p_begin; p < p_end; ++p) bead(p - p_begin, p, true);
         }
 
         // ============================ phase C: combine the chunks ===============================

@@ -7,11 +7,11 @@
 
 namespace pbr {
 
-template <int A, int K, int QM, typename T>
-static int launch_fused_one(const FusedArgs& args, cudaStream_t stream) {
+template <int A, int K, int QM, typename T, bool kTcq>
+static int launch_fused_kern(const FusedArgs& args, cudaStream_t stream) {
     const SmemPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S,
-                        args.qstride);
-    auto kern = pimc_fused_kernel<A, K, QM, T>;
+                        args.qstride, kTcq ? 1 : 0);
+    auto kern = pimc_fused_kernel<A, K, QM, T, kTcq>;
     static int configured = 0;    // dynamic shared memory opt-in already granted to this kernel
     if (plan.total_bytes > 48 * 1024 && plan.total_bytes > configured) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -30,6 +30,13 @@ static int launch_fused_one(const FusedArgs& args, cudaStream_t stream) {
     if (grid <= 0) return PBR_OK;
     kern<<<grid, kThreads, plan.total_bytes, stream>>>(args);
     return cudaGetLastError() == cudaSuccess ? PBR_OK : PBR_ERR_CUDA;
+}
+
+template <int A, int K, int QM, typename T>
+static int launch_fused_one(const FusedArgs& args, cudaStream_t stream) {
+    if constexpr (sizeof(T) == 4 && A >= 3)
+        if (args.tcq) return launch_fused_kern<A, K, QM, T, true>(args, stream);
+    return launch_fused_kern<A, K, QM, T, false>(args, stream);
 }
 
 template <int A>

@@ -308,20 +308,8 @@ __device__ __forceinline__ void mma_f16_ts(uint32_t tmem_d, uint32_t tmem_a, uin
         ::"r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
-// FP16 pair (x0, x1), x0 in the low half
-__device__ __forceinline__ uint32_t pack_f16x2(float x0, float x1) {
-    uint32_t r;
-    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(x1), "f"(x0));
-    return r;
-}
-
-// hi = FP16(x) and lo = FP16(x - hi) for two values, packed as FP16 pairs
-__device__ __forceinline__ void split_f16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
-    hi = pack_f16x2(x0, x1);
-    const __half2 h = *reinterpret_cast<const __half2*>(&hi);
-    const float2 hf = __half22float2(h);
-    lo = pack_f16x2(x0 - hf.x, x1 - hf.y);
-}
+using pbr::pack_f16x2;
+using pbr::split_f16x2;
 
 // bounded wait that gives up early once another role has recorded an error
 __device__ __forceinline__ bool mbar_wait_or_err(uint64_t* bar, uint32_t parity, volatile int* err) {
