@@ -72,8 +72,22 @@ int make_team_args(const pbr_model& m, int qmode, const void* q_in, int64_t X, u
 
 int team_smem(const pbr::TeamArgs& a, int qmode) {
     const pbr::TeamPlan plan(a.m.A, a.m.K, qmode, a.m.precision == 32 ? 4 : 8, a.m.N, a.m.P, a.S, a.G,
-                             a.qstride, a.rl);
+                             a.qstride, a.rl, a.tcq);
     return plan.total_bytes;
+}
+
+// B1's tensor-core quadratic for a single-model row-team launch: FP32, q drawn or given (not V),
+// 5-8 surfaces (one block per SM; the two-block build at 5-6 surfaces is kept when its tile
+// fits), from kTcqMinN modes, and only when its tables still fit the budget
+void choose_team_tcq(pbr::TeamArgs& a, int qmode, int smem_budget) {
+    using namespace pbr;
+    a.tcq = 0;
+    const pbr_model& m = a.m;
+    if (m.precision != 32 || qmode == kQ32V || m.A < 5 || m.A > 8 || m.N < kTcqMinN) return;
+    if ((m.A == 5 || m.A == 6) && team_smem(a, qmode) <= kTeamTwoBlockSmem) return;
+    a.tcq = 1;
+    const TeamPlan pt(m.A, m.K, qmode, 4, m.N, m.P, a.S, a.G, a.qstride, a.rl, 1);
+    if (pt.tcq_k == 0 || pt.total_bytes > smem_budget) a.tcq = 0;
 }
 
 int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
@@ -83,6 +97,7 @@ int run_team(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_
     TeamArgs a;
     const int rc = make_team_args(m, qmode, q_in, X, seed, offset, out, kMaxSmem, &a);
     if (rc != PBR_OK) return rc;
+    choose_team_tcq(a, qmode, kMaxSmem);
     a.vq = vq;
     a.vq_ld = vq_ld;
     switch (m.A) {

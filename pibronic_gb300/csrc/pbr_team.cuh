@@ -40,6 +40,7 @@ struct TeamArgs {
     int rl;         // bead record length
     const float* vq;  // kQ32V: V(q) (energies, linear, quadratic), row (sample * P + bead), A(A+1)/2 used columns
     int vq_ld;        // kQ32V: floats per row of vq
+    int tcq;          // 1: B1's quadratic part of V on the tensor cores (its tables, its instantiation)
 };
 
 __host__ __device__ inline int pow2_ceil(int x) {
@@ -55,14 +56,17 @@ struct TeamPlan {
     int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
     int alt;          // second buffer of combine slots (the split combine), or -1: none fits
     bool stage_ring;  // the ring factor fits the bead-record region (phase A copies it there)
+    int tcq_k;        // k-steps of B1's tensor-core quadratic (0: the FP32 pair loop)
     __host__ __device__ TeamPlan() : c(0), e(0), qq(0), rc(0), rec(0), src(0), q(0), qlo(0), beads(0),
-                                     lsums(0), total_bytes(0), alt(-1), stage_ring(false) {}
+                                     lsums(0), total_bytes(0), alt(-1), stage_ring(false), tcq_k(0) {}
     __host__ __device__ TeamPlan(int A, int K, int qm, int esz, int N, int P, int S, int G, int qstride,
-                                 int rl) {
+                                 int rl, int tcq = 0) {
         const int A2P = align_up(npair(A), 4);
         int o = 0;
         auto take = [&](int n) { int r = o; o = align_up(o + n, 4); return r; };
-        c = take((K + 1) * A); e = take(A2P); qq = take(qm == kQ32V ? 0 : npair(N) * A2P); rc = take(A);
+        tcq_k = (tcq && esz == 4 && qm != kQ32V && N >= kTcqMinN && qstride - 1 < 65536) ? tcq_ksteps(N) : 0;
+        c = take((K + 1) * A); e = take(A2P);
+        qq = take(qm == kQ32V ? 0 : (tcq_k ? tcq_words(N, A) : npair(N) * A2P)); rc = take(A);
         rec = take(N * rec_len(A, K));
         src = take(S);                                             // ints stored in the slot
         q = take(S * qstride);
@@ -80,8 +84,9 @@ struct TeamPlan {
     }
 };
 
-// Copy one model's tables into the CTA's shared memory (layout TeamPlan).
-template <int A, int K, int QM, typename T>
+// Copy one model's tables into the CTA's shared memory (layout TeamPlan; kTcq: the tensor-core
+// quadratic's tables in place of the packed coupling table).
+template <int A, int K, int QM, typename T, bool kTcq = false>
 __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
@@ -102,10 +107,15 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
         const T* g_rc = static_cast<const T*>(m.rho_c);   const T* g_rd = static_cast<const T*>(m.rho_d);
         for (int i = tid; i < (K + 1) * A; i += NT) s_c[i] = g_c[i];
         for (int i = tid; i < A2P; i += NT) s_e[i] = (i < A2) ? g_e[i] : T(0);
-        const int N2 = (QM == kQ32V) ? 0 : npair(N);
-        for (int i = tid; i < N2 * A2P; i += NT) {
-            const int row = i / A2P, col = i - row * A2P;
-            s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
+        if constexpr (kTcq) {
+            tcq_tables<A>(reinterpret_cast<const float*>(g_qq), N, row_stride(m.P), plan.tcq_k,
+                          reinterpret_cast<uint32_t*>(s_qq));
+        } else {
+            const int N2 = (QM == kQ32V) ? 0 : npair(N);
+            for (int i = tid; i < N2 * A2P; i += NT) {
+                const int row = i / A2P, col = i - row * A2P;
+                s_qq[i] = (col < A2) ? g_qq[row * A2 + col] : T(0);
+            }
         }
         for (int i = tid; i < A; i += NT) s_rc[i] = (i < nfill) ? g_rc[i] : T(0);
         for (int i = tid; i < N * MR; i += NT) {
@@ -128,7 +138,7 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
 // build targets; the two-block build (128 registers) uses the forms that need fewer registers:
 // the receiver combine, a two-step prefetch in the chains and, at 5 surfaces, a B2 that streams
 // the bead matrices column by column (at 6 surfaces that form measured slower than its spills).
-template <int A, int K, int QM, typename T, int MB = 1>
+template <int A, int K, int QM, typename T, int MB = 1, bool kTcq = false>
 __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int64_t base) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
@@ -234,172 +244,229 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
         }
 
         // ================================ phase B1: bead records ===============================
-        for (int it = tid; it < nvalid * P; it += NT) {
+        // record it = (sample s, bead p); on = a live record.  With the tensor-core quadratic every
+        // thread runs the same number of records (the warp's 32 rows go through the MMAs
+        // together); otherwise each thread takes its own records only.
+        int it_base = 0;           // first record of the current round (the uniform loop)
+        auto record = [&](const int it, const bool on) {
             const int s = it / P, p = it - s * P;
-            const int pn = (p + 1 == P) ? 0 : p + 1;
             const T* qs = s_q + s * args.qstride;
-            const T* ql = kLo ? s_ql + s * args.qstride : nullptr;
-            const int ip = qidx(0, p, rs), ipn = qidx(0, pn, rs);
+            const int ip = qidx(0, p, rs);
             T* rec_out = s_beads + static_cast<int64_t>(it) * RL;
-            T phv[K + 1][A], phr[A], v[A2P];
+            T v[A2P];
+            T qmax = T(0);
+            if (on) {
+                const int pn = (p + 1 == P) ? 0 : p + 1;
+                const T* ql = kLo ? s_ql + s * args.qstride : nullptr;
+                const int ipn = qidx(0, pn, rs);
+                T phv[K + 1][A], phr[A];
 #pragma unroll
-            for (int k = 0; k <= K; ++k)
+                for (int k = 0; k <= K; ++k)
 #pragma unroll
-                for (int a = 0; a < A; ++a) phv[k][a] = s_c[k * A + a];
+                    for (int a = 0; a < A; ++a) phv[k][a] = s_c[k * A + a];
 #pragma unroll
-            for (int a = 0; a < A; ++a) phr[a] = s_rc[a];
-            ldv(s_e, v);
-            T dsum[K + 1];
+                for (int a = 0; a < A; ++a) phr[a] = s_rc[a];
+                ldv(s_e, v);
+                T dsum[K + 1];
 #pragma unroll
-            for (int k = 0; k <= K; ++k) dsum[k] = T(0);
-            T rdsum = T(0);
-            for (int j = 0; j < N; ++j) {
-                const T* rec = s_rec + j * MR;
-                T cs[KP], th[KP], dv[AP], rdv[AP], rx[4], lr[A2P];
-                ldv(rec, cs);
-                ldv(rec + KP, th);
-                ldv(rec + 2 * KP, dv);
-                ldv(rec + 2 * KP + AP, rdv);
-                ldv(rec + 2 * KP + 2 * AP, rx);
-                ldv(rec + 2 * KP + 2 * AP + 4, lr);
-                const T qa = qs[ip + j * rs], qb = qs[ipn + j * rs];
-                T dq = qa - qb;
-                if (kLo) dq += ql[ip + j * rs] - ql[ipn + j * rs];
-                const T dq2 = dq * dq;
+                for (int k = 0; k <= K; ++k) dsum[k] = T(0);
+                T rdsum = T(0);
+                for (int j = 0; j < N; ++j) {
+                    const T* rec = s_rec + j * MR;
+                    T cs[KP], th[KP], dv[AP], rdv[AP], rx[4], lr[A2P];
+                    ldv(rec, cs);
+                    ldv(rec + KP, th);
+                    ldv(rec + 2 * KP, dv);
+                    ldv(rec + 2 * KP + AP, rdv);
+                    ldv(rec + 2 * KP + 2 * AP, rx);
+                    ldv(rec + 2 * KP + 2 * AP + 4, lr);
+                    const T qa = qs[ip + j * rs], qb = qs[ipn + j * rs];
+                    if constexpr (kTcq) qmax = max(qmax, dev_fabs(qa));
+                    T dq = qa - qb;
+                    if (kLo) dq += ql[ip + j * rs] - ql[ipn + j * rs];
+                    const T dq2 = dq * dq;
 #pragma unroll
-                for (int k = 0; k <= K; ++k) dsum[k] = fma(cs[k], dq2, dsum[k]);
-                rdsum = fma(rx[0], dq2, rdsum);
+                    for (int k = 0; k <= K; ++k) dsum[k] = fma(cs[k], dq2, dsum[k]);
+                    rdsum = fma(rx[0], dq2, rdsum);
 #pragma unroll
-                for (int a = 0; a < A; ++a) {
-                    const T ua = qa - dv[a], ub = qb - dv[a];
-                    const T sq = fma(ua, ua, ub * ub);
+                    for (int a = 0; a < A; ++a) {
+                        const T ua = qa - dv[a], ub = qb - dv[a];
+                        const T sq = fma(ua, ua, ub * ub);
 #pragma unroll
-                    for (int k = 0; k <= K; ++k) phv[k][a] = fma(-th[k], sq, phv[k][a]);
-                    if (a < nfill) {
-                        const T ra = qa - rdv[a], rb = qb - rdv[a];
-                        phr[a] = fma(-rx[1], fma(ra, ra, rb * rb), phr[a]);
+                        for (int k = 0; k <= K; ++k) phv[k][a] = fma(-th[k], sq, phv[k][a]);
+                        if (a < nfill) {
+                            const T ra = qa - rdv[a], rb = qb - rdv[a];
+                            phr[a] = fma(-rx[1], fma(ra, ra, rb * rb), phr[a]);
+                        }
+                    }
+#pragma unroll
+                    if (QM != kQ32V)
+#pragma unroll
+                        for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
+                }
+                T lmax;
+                {
+#pragma unroll
+                    for (int a = 0; a < A; ++a) {
+#pragma unroll
+                        for (int k = 0; k <= K; ++k) phv[k][a] -= dsum[k];
+                        phr[a] -= rdsum;
+                    }
+                    lmax = phv[0][0];
+#pragma unroll
+                    for (int a = 1; a < A; ++a) lmax = max(lmax, phv[0][a]);
+#pragma unroll
+                    for (int a = 0; a < A; ++a)
+                        if (a < nfill) lmax = max(lmax, phr[a]);
+                    rec_out[OFF_L] = lmax;
+#pragma unroll
+                    for (int a = 0; a < A; ++a) rec_out[OFF_R + a] = (a < nfill) ? phr[a] - lmax : T(0);
+#pragma unroll
+                    for (int a = 0; a < A; ++a) {
+                        T ek[K + 1];
+                        ek[0] = T(1);
+#pragma unroll
+                        for (int k = 1; k <= K; ++k) {
+                            T acc = T(0);
+#pragma unroll
+                            for (int i = 1; i <= k; ++i) acc = fma(T(i) * phv[i][a], ek[k - i], acc);
+                            ek[k] = acc * (T(1) / T(k));
+                        }
+                        const T e0 = dev_exp<T>(phv[0][a] - lmax);
+#pragma unroll
+                        for (int k = 0; k <= K; ++k) rec_out[OFF_O + k * A + a] = e0 * ek[k];
                     }
                 }
+                if (QM == kQ32V) {
+                    const float* vr = args.vq + ((base + s) * static_cast<int64_t>(P) + p) * args.vq_ld;
 #pragma unroll
-                if (QM != kQ32V)
-#pragma unroll
-                    for (int pr = 0; pr < A2; ++pr) v[pr] = fma(lr[pr], qa, v[pr]);
-            }
-            T lmax;
-            {
-#pragma unroll
-                for (int a = 0; a < A; ++a) {
-#pragma unroll
-                    for (int k = 0; k <= K; ++k) phv[k][a] -= dsum[k];
-                    phr[a] -= rdsum;
-                }
-                lmax = phv[0][0];
-#pragma unroll
-                for (int a = 1; a < A; ++a) lmax = max(lmax, phv[0][a]);
-#pragma unroll
-                for (int a = 0; a < A; ++a)
-                    if (a < nfill) lmax = max(lmax, phr[a]);
-                rec_out[OFF_L] = lmax;
-#pragma unroll
-                for (int a = 0; a < A; ++a) rec_out[OFF_R + a] = (a < nfill) ? phr[a] - lmax : T(0);
-#pragma unroll
-                for (int a = 0; a < A; ++a) {
-                    T ek[K + 1];
-                    ek[0] = T(1);
-#pragma unroll
-                    for (int k = 1; k <= K; ++k) {
-                        T acc = T(0);
-#pragma unroll
-                        for (int i = 1; i <= k; ++i) acc = fma(T(i) * phv[i][a], ek[k - i], acc);
-                        ek[k] = acc * (T(1) / T(k));
+                    for (int pr = 0; pr < A2; pr += 4) {
+                        const float4 w = *reinterpret_cast<const float4*>(vr + pr);
+                        v[pr] = T(w.x);
+                        if (pr + 1 < A2) v[pr + 1] = T(w.y);
+                        if (pr + 2 < A2) v[pr + 2] = T(w.z);
+                        if (pr + 3 < A2) v[pr + 3] = T(w.w);
                     }
-                    const T e0 = dev_exp<T>(phv[0][a] - lmax);
-#pragma unroll
-                    for (int k = 0; k <= K; ++k) rec_out[OFF_O + k * A + a] = e0 * ek[k];
                 }
             }
-            if (QM == kQ32V) {
-                const float* vr = args.vq + ((base + s) * static_cast<int64_t>(P) + p) * args.vq_ld;
+            if constexpr (QM != kQ32V) {
+                bool quad_done = false;
+                if constexpr (kTcq) {
+                    // tensor cores, unless a record of the warp has a coordinate beyond FP16's
+                    // range for the products (then the FP32 loop over the global table)
+                    if (!__any_sync(0xffffffffu, on && !(qmax <= T(kTcqMaxQ)))) {
+                        int rec[4];
+                        const int itw = it_base + (tid & ~31), nrec = nvalid * P;
 #pragma unroll
-                for (int pr = 0; pr < A2; pr += 4) {
-                    const float4 w = *reinterpret_cast<const float4*>(vr + pr);
-                    v[pr] = T(w.x);
-                    if (pr + 1 < A2) v[pr + 1] = T(w.y);
-                    if (pr + 2 < A2) v[pr + 2] = T(w.z);
-                    if (pr + 3 < A2) v[pr + 3] = T(w.w);
+                        for (int r = 0; r < 4; ++r) {
+                            int ir = itw + 16 * (r >> 1) + 8 * (r & 1) + (lane >> 2);   // fragment rows: lane / 4 (+ 8)
+                            ir = ir < nrec ? ir : 0;
+                            const int sr = ir / P, pr_ = ir - sr * P;
+                            rec[r] = plan.q + sr * args.qstride + qidx(0, pr_, rs);
+                        }
+                        float vq[A2];
+                        tcq_quadratic<A>(reinterpret_cast<const uint32_t*>(s_qq), plan.tcq_k,
+                                         reinterpret_cast<const float*>(sm), rec, lane, vq);
+#pragma unroll
+                        for (int pr = 0; pr < A2; ++pr) v[pr] += vq[pr];
+                    } else if (on) {
+                        const float* gq = static_cast<const float*>(m.vib_qq);
+                        const int N2 = npair(N);
+                        int od = 0, oe = 0;
+                        for (int row = 0; row < N2; ++row) {
+                            const T w = qs[ip + od] * qs[ip + oe];
+#pragma unroll
+                            for (int pr = 0; pr < A2; ++pr) v[pr] = fma(__ldg(gq + row * A2 + pr), w, v[pr]);
+                            const bool wrap = (oe == od);
+                            od = wrap ? od + rs : od;
+                            oe = wrap ? 0 : oe + rs;
+                        }
+                    }
+                    quad_done = true;
                 }
-            } else {
-                // one flat loop over the mode pairs (d, e <= d) in table order, unrolled so several
-                // pairs' loads are in flight together
-                if constexpr (A >= kFlatPairsMinA) {
-                    const int N2 = npair(N);
-                    int od = 0, oe = 0;                  // offsets d * rs, e * rs of the pair (d, e)
+                if (on && !quad_done) {
+                    // one flat loop over the mode pairs (d, e <= d) in table order, unrolled so
+                    // several pairs' loads are in flight together
+                    if constexpr (A >= kFlatPairsMinA) {
+                        const int N2 = npair(N);
+                        int od = 0, oe = 0;                  // offsets d * rs, e * rs of the pair (d, e)
 #pragma unroll 4
-                    for (int row = 0; row < N2; ++row) {
-                        const T w = qs[ip + od] * qs[ip + oe];
-                        T qrow[A2P];
-                        ldv(s_qq + row * A2P, qrow);
-#pragma unroll
-                        for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
-                        const bool wrap = (oe == od);        // e == d: next row starts (d + 1, 0)
-                        od = wrap ? od + rs : od;
-                        oe = wrap ? 0 : oe + rs;
-                    }
-                } else {
-                    int row = 0;
-                    for (int d = 0; d < N; ++d) {
-                        const T qd = qs[ip + d * rs];
-                        for (int e = 0; e <= d; ++e, ++row) {
-                            const T w = qd * qs[ip + e * rs];
+                        for (int row = 0; row < N2; ++row) {
+                            const T w = qs[ip + od] * qs[ip + oe];
                             T qrow[A2P];
                             ldv(s_qq + row * A2P, qrow);
 #pragma unroll
                             for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                            const bool wrap = (oe == od);        // e == d: next row starts (d + 1, 0)
+                            od = wrap ? od + rs : od;
+                            oe = wrap ? 0 : oe + rs;
+                        }
+                    } else {
+                        int row = 0;
+                        for (int d = 0; d < N; ++d) {
+                            const T qd = qs[ip + d * rs];
+                            for (int e = 0; e <= d; ++e, ++row) {
+                                const T w = qd * qs[ip + e * rs];
+                                T qrow[A2P];
+                                ldv(s_qq + row * A2P, qrow);
+#pragma unroll
+                                for (int pr = 0; pr < A2; ++pr) v[pr] = fma(qrow[pr], w, v[pr]);
+                            }
                         }
                     }
                 }
             }
-            if constexpr (sizeof(T) == 4 && A >= kExpmMinA && A <= kTeamExpmMaxA) {
-                // M = exp(-tau V) by scaling and squaring in registers (see expm_neg_tau)
-                float vp[A2], X[A2], f;
+            if (on) {
+                if constexpr (sizeof(T) == 4 && A >= kExpmMinA && A <= kTeamExpmMaxA) {
+                    // M = exp(-tau V) by scaling and squaring in registers (see expm_neg_tau)
+                    float vp[A2], X[A2], f;
 #pragma unroll
-                for (int i = 0; i < A2; ++i) vp[i] = v[i];
-                rec_out[OFF_N] = T(expm_neg_tau_packed<A>(vp, static_cast<float>(m.tau), X, f));
+                    for (int i = 0; i < A2; ++i) vp[i] = v[i];
+                    rec_out[OFF_N] = T(expm_neg_tau_packed<A>(vp, static_cast<float>(m.tau), X, f));
 #pragma unroll
-                for (int b = 0; b < A; ++b)
+                    for (int b = 0; b < A; ++b)
 #pragma unroll
-                    for (int c = 0; c < A; ++c) rec_out[b * A + c] = f * X[sym_index(b, c)];
-            } else {
-                T am[A][A], u[A][A];
+                        for (int c = 0; c < A; ++c) rec_out[b * A + c] = f * X[sym_index(b, c)];
+                } else {
+                    T am[A][A], u[A][A];
 #pragma unroll
-                for (int b = 0; b < A; ++b)
+                    for (int b = 0; b < A; ++b)
 #pragma unroll
-                    for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
+                        for (int c = 0; c <= b; ++c) { am[b][c] = v[pair_index(b, c)]; am[c][b] = am[b][c]; }
 #pragma unroll
-                for (int b = 0; b < A; ++b)
+                    for (int b = 0; b < A; ++b)
 #pragma unroll
-                    for (int c = 0; c < A; ++c) u[b][c] = (b == c) ? T(1) : T(0);
-                jacobi_accumulate<T, A>(am, u, sizeof(T) == 4 ? 12 : 16);
-                T t[A];
-                T tmax = -tau_l2 * am[0][0];
+                        for (int c = 0; c < A; ++c) u[b][c] = (b == c) ? T(1) : T(0);
+                    jacobi_accumulate<T, A>(am, u, sizeof(T) == 4 ? 12 : 16);
+                    T t[A];
+                    T tmax = -tau_l2 * am[0][0];
 #pragma unroll
-                for (int i = 0; i < A; ++i) { t[i] = -tau_l2 * am[i][i]; tmax = max(tmax, t[i]); }
-                const int n2 = static_cast<int>(floor(tmax));
-                rec_out[OFF_N] = T(n2);
-                T ev[A];
+                    for (int i = 0; i < A; ++i) { t[i] = -tau_l2 * am[i][i]; tmax = max(tmax, t[i]); }
+                    const int n2 = static_cast<int>(floor(tmax));
+                    rec_out[OFF_N] = T(n2);
+                    T ev[A];
 #pragma unroll
-                for (int i = 0; i < A; ++i) ev[i] = dev_exp2<T>(t[i] - T(n2));
+                    for (int i = 0; i < A; ++i) ev[i] = dev_exp2<T>(t[i] - T(n2));
 #pragma unroll
-                for (int b = 0; b < A; ++b)
+                    for (int b = 0; b < A; ++b)
 #pragma unroll
-                    for (int c = 0; c <= b; ++c) {
-                        T acc = T(0);
+                        for (int c = 0; c <= b; ++c) {
+                            T acc = T(0);
 #pragma unroll
-                        for (int i = 0; i < A; ++i) acc = fma(u[b][i] * ev[i], u[c][i], acc);
-                        rec_out[b * A + c] = acc;
-                        rec_out[c * A + b] = acc;
-                    }
+                            for (int i = 0; i < A; ++i) acc = fma(u[b][i] * ev[i], u[c][i], acc);
+                            rec_out[b * A + c] = acc;
+                            rec_out[c * A + b] = acc;
+                        }
+                }
             }
+        };
+        if constexpr (kTcq) {
+            for (; it_base < nvalid * P; it_base += NT) {
+                const int it = it_base + tid;
+                record(it < nvalid * P ? it : 0, it < nvalid * P);
+            }
+        } else {
+            for (int it = tid; it < nvalid * P; it += NT) record(it, true);
         }
         __syncthreads();
 
@@ -744,17 +811,19 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
 template <int A> constexpr int team_min_blocks() { return A <= 4 ? 2 : 1; }
 constexpr int kTeamTwoBlockSmem = 113 * 1024;
 
-template <int A, int K, int QM, typename T, int MB = team_min_blocks<A>()>
+// kTcq: the instantiation with B1's quadratic part of V on the tensor cores (launched when
+// args.tcq is set; one block per SM only)
+template <int A, int K, int QM, typename T, int MB = team_min_blocks<A>(), bool kTcq = false>
 __global__ void __launch_bounds__(kTeamThreads, MB) pimc_team_kernel(const TeamArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* sm = reinterpret_cast<T*>(smem_raw);
     const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
-                        args.qstride, args.rl);
-    team_load_tables<A, K, QM, T>(args.m, sm, plan);
+                        args.qstride, args.rl, kTcq ? 1 : 0);
+    team_load_tables<A, K, QM, T, kTcq>(args.m, sm, plan);
     __syncthreads();
     for (int64_t base = static_cast<int64_t>(blockIdx.x) * args.S; base < args.X;
          base += static_cast<int64_t>(gridDim.x) * args.S)
-        team_tile<A, K, QM, T, MB>(args, sm, plan, base);
+        team_tile<A, K, QM, T, MB, kTcq>(args, sm, plan, base);
 }
 
 // ---------------------------------------------------------------------------------------------

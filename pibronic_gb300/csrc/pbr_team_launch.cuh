@@ -11,9 +11,9 @@ namespace pbr {
 template <int A, typename T>
 constexpr bool team_two_block_build() { return (A == 5 || A == 6) && sizeof(T) == 4; }
 
-template <int A, int K, int QM, typename T, int MB>
+template <int A, int K, int QM, typename T, int MB, bool kTcq = false>
 static int launch_team_kern(const TeamArgs& args, int smem_bytes, cudaStream_t stream) {
-    auto kern = pimc_team_kernel<A, K, QM, T, MB>;
+    auto kern = pimc_team_kernel<A, K, QM, T, MB, kTcq>;
     static int configured = 0;
     if (smem_bytes > 48 * 1024 && smem_bytes > configured) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) != cudaSuccess)
@@ -35,7 +35,9 @@ static int launch_team_kern(const TeamArgs& args, int smem_bytes, cudaStream_t s
 template <int A, int K, int QM, typename T>
 static int launch_team_one(const TeamArgs& args, cudaStream_t stream) {
     const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
-                        args.qstride, args.rl);
+                        args.qstride, args.rl, args.tcq);
+    if constexpr (sizeof(T) == 4 && QM != kQ32V && A >= 3 && team_min_blocks<A>() == 1)
+        if (args.tcq) return launch_team_kern<A, K, QM, T, 1, true>(args, plan.total_bytes, stream);
     if constexpr (team_two_block_build<A, T>())
         if (plan.total_bytes <= kTeamTwoBlockSmem) return launch_team_kern<A, K, QM, T, 2>(args, plan.total_bytes, stream);
     return launch_team_kern<A, K, QM, T, team_min_blocks<A>()>(args, plan.total_bytes, stream);
