@@ -232,8 +232,11 @@ int pbr_sample_q(const pbr_model* model, uint64_t seed, uint64_t offset, int64_t
         a.G *= 2;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (bytes > kMaxSmem) {
-        // samples too large to stage whole in shared memory: the row-streaming form
+    if (bytes > kMaxSmem || m.precision == 32) {
+        // FP32: the row-streaming form (one mode of 32 samples per warp, lane = sample), the same
+        // bits as the staged form and measured 1.8-4.1x faster on GB300 (A = 3-8, N = 6-20,
+        // P = 16-256: more warps per SM hide the chains' latency); FP64 samples too large to
+        // stage have no form
         if (m.precision != 32) return PBR_ERR_UNSUPPORTED;
         int dev = 0, sms = 0;
         PBR_CUDA_CHECK_RET(cudaGetDevice(&dev));
