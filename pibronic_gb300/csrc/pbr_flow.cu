@@ -65,15 +65,17 @@ int resident_blocks(K kern, int threads, int bytes) {
 // prepare: y[x][j*nsel + s] = (sum_p B_ps (q_jp - c_j)) * inv_sigma[j*nsel + s],
 //          U[x] = sum_j (q_j - c_j)^T Lambda_j (q_j - c_j) - sum |y|^2
 // Lambda_j = 2 coth I - csch C evaluated as sum_p csch (dx)^2 + 2 tanh(tau w/2) x_p^2.
-// One warp per (sample); lanes over beads.  FP32 within a mode (the lanes' partial sums and their
-// shuffle reduction), FP64 only across modes: the FP64 pipe of this part runs at a small fraction
-// of the FP32 rate, and FP64 shuffles and products per mode made the kernel FP64-bound.
+// One thread per (sample, mode), reading the mode's P beads in order (16-byte loads when P % 4
+// == 0): the ring energy and the nsel projections of the mode in FP32, no shuffles; a block holds
+// whole samples (floor(blockDim / N) of them), whose modes' terms are summed in FP64 through
+// shared memory.  (The warp-per-sample form with a shuffle reduction per mode took 4-5x longer.)
 // ---------------------------------------------------------------------------------------------
 __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int N, int P, int nsel,
                                     const double* __restrict__ center, const double* __restrict__ inv_sigma,
                                     const double* __restrict__ rho_csch, const double* __restrict__ rho_tanh2,
                                     float* __restrict__ y, double* __restrict__ U) {
-    extern __shared__ float basis[];            // [nsel][P] ring basis columns, then per mode (FP32):
+    extern __shared__ double part[];            // [blockDim] per-thread FP64 terms, then (FP32):
+    float* basis = reinterpret_cast<float*>(part + blockDim.x);   // [nsel][P] ring basis columns
     float* s_isig = basis + nsel * P;           // inv_sigma [N][nsel]
     float* s_mode = s_isig + N * nsel;          // [N][4]: center, csch, 2 tanh(tau w / 2), 0
     const double inv_sqrt_p = 1.0 / sqrt(static_cast<double>(P));
@@ -96,45 +98,64 @@ __global__ void flow_prepare_kernel(const float* __restrict__ q, int64_t X, int 
         s_mode[4 * j + 3] = 0.f;
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int64_t gw = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + warp;
-    const int64_t nw = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
-    for (int64_t x = gw; x < X; x += nw) {
-        double quad_total = 0.0;
-        float ysq = 0.0f;
-        for (int j = 0; j < N; ++j) {
+    const int spb = static_cast<int>(blockDim.x) / N;            // whole samples per block
+    const int t = threadIdx.x, sl = t / N, j = t - sl * N;
+    const bool vec = (P & 3) == 0 && (reinterpret_cast<uintptr_t>(q) & 15) == 0;
+    for (int64_t x0 = static_cast<int64_t>(blockIdx.x) * spb; x0 < X; x0 += static_cast<int64_t>(gridDim.x) * spb) {
+        const int64_t x = x0 + sl;
+        double term = 0.0;
+        if (sl < spb && x < X) {
             const float* qj = q + (x * N + j) * static_cast<int64_t>(P);
             const float c = s_mode[4 * j], ch = s_mode[4 * j + 1], th2 = s_mode[4 * j + 2];
-            float quad = 0.0f;
-            float proj[8];
+            float quad = 0.f, proj[8];
 #pragma unroll
-            for (int s = 0; s < 8; ++s) proj[s] = 0.0f;
-            for (int p = lane; p < P; p += 32) {
-                const float xp = qj[p] - c;
-                const float xn = qj[(p + 1 == P) ? 0 : p + 1] - c;
-                const float d = xp - xn;
-                quad = fmaf(ch * d, d, fmaf(th2 * xp, xp, quad));
+            for (int s = 0; s < 8; ++s) proj[s] = 0.f;
+            const float xfirst = qj[0] - c;
+            float xprev = xfirst;
+            auto bead = [&](int p, float xp) {
+                const float d = xprev - xp;          // x_{p-1} - x_p (the pair (p-1, p) of the ring)
+                quad = fmaf(th2 * xp, xp, quad);
+                if (p > 0) quad = fmaf(ch * d, d, quad);
 #pragma unroll
                 for (int s = 0; s < 8; ++s)
                     if (s < nsel) proj[s] = fmaf(basis[s * P + p], xp, proj[s]);
+                xprev = xp;
+            };
+            if (vec) {
+                const float4* q4 = reinterpret_cast<const float4*>(qj);
+                for (int p4 = 0; p4 < P / 4; ++p4) {
+                    const float4 v = q4[p4];
+                    bead(4 * p4, v.x - c);
+                    bead(4 * p4 + 1, v.y - c);
+                    bead(4 * p4 + 2, v.z - c);
+                    bead(4 * p4 + 3, v.w - c);
+                }
+            } else {
+                for (int p = 0; p < P; ++p) bead(p, qj[p] - c);
             }
-#pragma unroll
-            for (int o = 16; o >= 1; o >>= 1) {
-                quad += __shfl_xor_sync(0xffffffffu, quad, o);
-#pragma unroll
-                for (int s = 0; s < 8; ++s)
-                    if (s < nsel) proj[s] += __shfl_xor_sync(0xffffffffu, proj[s], o);   // nsel is uniform
+            {
+                const float d = xprev - xfirst;      // the ring's closing pair (P-1, 0)
+                quad = fmaf(ch * d, d, quad);
             }
-            quad_total += static_cast<double>(quad);
+            float ysq = 0.f;
+            float* yo = y + x * static_cast<int64_t>(N * nsel) + j * nsel;
 #pragma unroll
             for (int s = 0; s < 8; ++s) {
                 if (s >= nsel) break;
                 const float v = proj[s] * s_isig[j * nsel + s];
                 ysq = fmaf(v, v, ysq);
-                if (lane == 0) y[x * static_cast<int64_t>(N * nsel) + j * nsel + s] = v;
+                yo[s] = v;
             }
+            term = static_cast<double>(quad) - static_cast<double>(ysq);
         }
-        if (lane == 0) U[x] = quad_total - static_cast<double>(ysq);
+        part[t] = term;
+        __syncthreads();
+        if (t < spb && x0 + t < X) {
+            double sum = 0.0;
+            for (int jj = 0; jj < N; ++jj) sum += part[t * N + jj];
+            U[x0 + t] = sum;
+        }
+        __syncthreads();
     }
 }
 
@@ -998,11 +1019,15 @@ int pbr_flow_prepare(const float* q, int64_t X, int32_t N, int32_t P, int32_t ns
     if (X < 0 || N < 1 || P < 3 || P > 4096 || nsel < 1 || nsel > 8 || nsel > 1 + 2 * ((P - 1) / 2))
         return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
-    const int threads = 128;
-    const int bytes = static_cast<int>(sizeof(float)) * (nsel * P + N * nsel + 4 * N);
+    const int threads = 256;
+    if (N > threads) return PBR_ERR_UNSUPPORTED;
+    const int bytes = static_cast<int>(sizeof(double)) * threads +
+                      static_cast<int>(sizeof(float)) * (nsel * P + N * nsel + 4 * N);
     if (resident_blocks(flow_prepare_kernel, threads, bytes) < 1) return PBR_ERR_UNSUPPORTED;
-    flow_prepare_kernel<<<grid_for(X * 32, threads), threads, bytes, static_cast<cudaStream_t>(stream)>>>(
-        q, X, N, P, nsel, center, inv_sigma, rho_csch, rho_tanh2, y, U);
+    const int64_t spb = threads / N;
+    flow_prepare_kernel<<<grid_for((X + spb - 1) / spb * threads, threads), threads, bytes,
+                          static_cast<cudaStream_t>(stream)>>>(q, X, N, P, nsel, center, inv_sigma, rho_csch,
+                                                               rho_tanh2, y, U);
     return status();
 }
 
