@@ -792,6 +792,27 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
 // splits' partials are added in split order by gemm_tn_reduce, so the result is deterministic.
 constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
 constexpr int kGemmRowsPerSplit = 256;
+
+// TF32 hi and lo parts of x (round to nearest), as the 32-bit patterns mma.sync takes
+__device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(hi) : "f"(x));
+    const float r = x - __uint_as_float(hi);
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(lo) : "f"(r));
+}
+
+// D (16 x 8, FP32) += A (16 x 8) B (8 x 8), TF32 operands
+__device__ __forceinline__ void mma_tf32_1688(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Weight-gradient GEMM C = A^T B over the batch (A [X][M], B [X][N] row-major), split over the
+// batch: each block stages kGBK batch rows of a 64 x 64 output tile in shared memory and its 8
+// warps multiply them on the tensor cores (mma.sync m16n8k8, TF32 hi/lo split of both operands,
+// three MMAs per step: about FP32 accuracy); warp w owns rows 16 (w % 4) .. + 15 and columns
+// 32 (w / 4) .. + 31 of the tile.
 __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restrict__ A, const float* __restrict__ B,
                                                        int64_t X, int M, int N, int64_t chunk, int with_colsum,
                                                        float* __restrict__ part) {
@@ -802,7 +823,9 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
     const bool colsum = with_colsum && blockIdx.x == 0;
     float bs[4] = {0.f, 0.f, 0.f, 0.f};
     const int tm = blockIdx.x * kGBM, tn = blockIdx.y * kGBN, split = blockIdx.z;
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;       // 16 x 16 threads, 4 x 4 outputs each
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int wm = 16 * (warp & 3), wn = 32 * (warp >> 2);
     float acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -824,29 +847,35 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
                 bs[0] += v.x; bs[1] += v.y; bs[2] += v.z; bs[3] += v.w;
             }
         }
-#pragma unroll 8
-        for (int k = 0; k < kGBK; ++k) {
-            const float4 a = *reinterpret_cast<const float4*>(&sa[k][ty * 4]);
-            const float4 b = *reinterpret_cast<const float4*>(&sb[k][tx * 4]);
-            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+        for (int k0 = 0; k0 < kGBK; k0 += 8) {
+            // A^T fragment: rows = output rows m, columns = batch rows k
+            uint32_t ah[4], al[4];
+            split_tf32(sa[k0 + t][wm + g], ah[0], al[0]);
+            split_tf32(sa[k0 + t][wm + g + 8], ah[1], al[1]);
+            split_tf32(sa[k0 + t + 4][wm + g], ah[2], al[2]);
+            split_tf32(sa[k0 + t + 4][wm + g + 8], ah[3], al[3]);
 #pragma unroll
-                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+            for (int nt = 0; nt < 4; ++nt) {
+                uint32_t bh0, bl0, bh1, bl1;
+                split_tf32(sb[k0 + t][wn + 8 * nt + g], bh0, bl0);
+                split_tf32(sb[k0 + t + 4][wn + 8 * nt + g], bh1, bl1);
+                mma_tf32_1688(acc[nt], ah, bh0, bh1);
+                mma_tf32_1688(acc[nt], ah, bl0, bl1);
+                mma_tf32_1688(acc[nt], al, bh0, bh1);
+            }
         }
         __syncthreads();
     }
-    // partials: [split][M + 1][N], row M = the column sums
+    // partials: [split][M + 1][N], row M = the column sums; fragment element (row g / g + 8,
+    // columns 2 t, 2 t + 1) of each 16 x 8 tile
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int m = tm + ty * 4 + i;
-        if (m >= M) continue;
+    for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int n = tn + tx * 4 + j;
-            if (n < N) part[(static_cast<int64_t>(split) * (M + 1) + m) * N + n] = acc[i][j];
+        for (int e = 0; e < 4; ++e) {
+            const int m = tm + wm + g + 8 * (e >> 1), n = tn + wn + 8 * nt + 2 * t + (e & 1);
+            if (m < M && n < N) part[(static_cast<int64_t>(split) * (M + 1) + m) * N + n] = acc[nt][e];
         }
-    }
     if (colsum) {                                  // block-uniform
 #pragma unroll
         for (int j = 0; j < 4; ++j) sa[ty][tx * 4 + j] = bs[j];    // sa is free after the last tile
@@ -854,10 +883,10 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
         if (ty == 0) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                float t = 0.f;
-                for (int r = 0; r < 16; ++r) t += sa[r][tx * 4 + j];
+                float tt = 0.f;
+                for (int r = 0; r < 16; ++r) tt += sa[r][tx * 4 + j];
                 const int n = tn + tx * 4 + j;
-                if (n < N) part[(static_cast<int64_t>(split) * (M + 1) + M) * N + n] = t;
+                if (n < N) part[(static_cast<int64_t>(split) * (M + 1) + M) * N + n] = tt;
             }
         }
     }
