@@ -8,7 +8,7 @@
 namespace pbr {
 template <int A> int launch_fused(int, int, int, const FusedArgs&, cudaStream_t);
 template <int A> int launch_team(int, int, int, const TeamArgs&, cudaStream_t);
-template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, cudaStream_t);
+template <int A> int launch_team_batch(int, const TeamBatchItem*, int, int64_t, int, int, int, cudaStream_t);
 int tc_quadratic_cols(int A);
 int tc_quadratic_kdim(int N);
 int64_t tc_packed_floats(int N, int A);
@@ -274,7 +274,7 @@ constexpr int kBatchMaxGroups = 32;
 // row-team launch (up to 4 surfaces the chunk form is 2.2-3x faster per sample; the launches
 // are short enough to sit in the same CUDA graph)
 struct BatchGroup {
-    int32_t A, K, n_items, smem_bytes, chunked, pad;
+    int32_t A, K, n_items, smem_bytes, chunked, tcq;
     int64_t first_item, total_tiles;
 };
 struct BatchHeader {
@@ -301,11 +301,13 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->grid_cap = grid_cap;
     int n = 0;
-    // group by (A, K) in increasing A, and at 5-6 surfaces by whether two tiles fit an SM (those
-    // models run the two-block build); within a group keep the caller's order
+    // group by (A, K) in increasing A; at 5-6 surfaces by whether two tiles fit an SM (those
+    // models run the two-block build); of the one-block models, those whose bead records take
+    // the tensor-core quadratic (5-8 surfaces, from 16 modes, tables within the budget) form
+    // their own group (cls 2); within a group keep the caller's order
     for (int A = 1; A <= PBR_MAX_A; ++A)
         for (int K = 0; K <= 4; K += 4)
-        for (int cls = 0; cls < 2; ++cls) {
+        for (int cls = 0; cls < 3; ++cls) {
             const int first = n;
             int64_t tiles = 0;
             int smem = 0;
@@ -327,7 +329,9 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
                     rc = make_team_args(m, kSample, nullptr, X[i], seeds[i], offsets[i], &outs[i], kMaxSmem, &a);
                 if (rc != PBR_OK) return rc;
                 const bool two = (A == 5 || A == 6) && team_smem(a, kSample) <= kTeamTwoBlockSmem;
-                if ((cls == 0) != two) continue;
+                if (!two) choose_team_tcq(a, kSample, budget);
+                const int c = two ? 0 : (a.tcq ? 2 : 1);
+                if (c != cls) continue;
                 TeamBatchItem& it = items[n];
                 it.a = a;
                 it.tile_begin = tiles;
@@ -341,6 +345,7 @@ int pbr_batch_pack(const pbr_model* models, const uint64_t* seeds, const uint64_
                 BatchGroup& g = hdr->groups[hdr->n_groups++];
                 g.A = A; g.K = K; g.n_items = n - first; g.smem_bytes = smem;
                 g.chunked = chunked ? 1 : 0;
+                g.tcq = cls == 2 ? 1 : 0;
                 g.first_item = first; g.total_tiles = tiles;
             }
         }
@@ -373,14 +378,14 @@ int pbr_sample_eval_batch(const void* host_blob, const void* device_blob, void* 
         const TeamBatchItem* gitems = items + g.first_item;
         int rc = PBR_ERR_UNSUPPORTED;
         switch (g.A) {
-            case 1: rc = launch_team_batch<1>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 2: rc = launch_team_batch<2>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 3: rc = launch_team_batch<3>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 4: rc = launch_team_batch<4>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 5: rc = launch_team_batch<5>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 6: rc = launch_team_batch<6>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 7: rc = launch_team_batch<7>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
-            case 8: rc = launch_team_batch<8>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, st); break;
+            case 1: rc = launch_team_batch<1>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 2: rc = launch_team_batch<2>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 3: rc = launch_team_batch<3>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 4: rc = launch_team_batch<4>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 5: rc = launch_team_batch<5>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 6: rc = launch_team_batch<6>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 7: rc = launch_team_batch<7>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
+            case 8: rc = launch_team_batch<8>(g.K, gitems, g.n_items, g.total_tiles, g.smem_bytes, hdr->grid_cap, g.tcq, st); break;
             default: break;
         }
         if (rc != PBR_OK) return rc;

@@ -838,7 +838,7 @@ struct TeamBatchItem {
     int64_t tile_begin;       // first tile of this model in the launch
 };
 
-template <int A, int K, int MB = team_min_blocks<A>()>
+template <int A, int K, int MB = team_min_blocks<A>(), bool kTcq = false>
 __global__ void __launch_bounds__(kTeamThreads, MB)
 pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int64_t total_tiles) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -853,12 +853,12 @@ pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int
         }
         const TeamArgs& a = items[lo].a;
         if (lo != cur) {
-            plan = TeamPlan(A, K, kSample, 4, a.m.N, a.m.P, a.S, a.G, a.qstride, a.rl);
-            team_load_tables<A, K, kSample, float>(a.m, sm, plan);
+            plan = TeamPlan(A, K, kSample, 4, a.m.N, a.m.P, a.S, a.G, a.qstride, a.rl, kTcq ? 1 : 0);
+            team_load_tables<A, K, kSample, float, kTcq>(a.m, sm, plan);
             __syncthreads();
             cur = lo;
         }
-        team_tile<A, K, kSample, float, MB>(a, sm, plan, (t - items[lo].tile_begin) * a.S);
+        team_tile<A, K, kSample, float, MB, kTcq>(a, sm, plan, (t - items[lo].tile_begin) * a.S);
     }
 }
 
@@ -867,6 +867,6 @@ int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStrea
 
 template <int A>
 int launch_team_batch(int K, const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
-                      int grid_cap, cudaStream_t stream);
+                      int grid_cap, int tcq, cudaStream_t stream);
 
 }  // namespace pbr

@@ -66,10 +66,10 @@ int launch_team(int K, int qmode, int precision, const TeamArgs& args, cudaStrea
     return launch_team_one<A, 4, kQ64, double>(args, stream);
 }
 
-template <int A, int K, int MB>
+template <int A, int K, int MB, bool kTcq = false>
 static int launch_team_batch_kern(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
                                   int grid_cap, cudaStream_t stream) {
-    auto kern = pimc_team_batch_kernel<A, K, MB>;
+    auto kern = pimc_team_batch_kernel<A, K, MB, kTcq>;
     if (smem_bytes > 48 * 1024 &&
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) != cudaSuccess)
         return PBR_ERR_UNSUPPORTED;
@@ -87,7 +87,10 @@ static int launch_team_batch_kern(const TeamBatchItem* items, int n_items, int64
 
 template <int A, int K>
 static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
-                                 int grid_cap, cudaStream_t stream) {
+                                 int grid_cap, int tcq, cudaStream_t stream) {
+    // a group of models on the tensor-core quadratic (one block per SM, 3+ surfaces)
+    if constexpr (A >= 3 && team_min_blocks<A>() == 1)
+        if (tcq) return launch_team_batch_kern<A, K, 1, true>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
     if constexpr (team_two_block_build<A, float>())
         if (smem_bytes <= kTeamTwoBlockSmem)
             return launch_team_batch_kern<A, K, 2>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
@@ -97,9 +100,9 @@ static int launch_team_batch_one(const TeamBatchItem* items, int n_items, int64_
 
 template <int A>
 int launch_team_batch(int K, const TeamBatchItem* items, int n_items, int64_t total_tiles, int smem_bytes,
-                      int grid_cap, cudaStream_t stream) {
-    if (K == 0) return launch_team_batch_one<A, 0>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
-    return launch_team_batch_one<A, 4>(items, n_items, total_tiles, smem_bytes, grid_cap, stream);
+                      int grid_cap, int tcq, cudaStream_t stream) {
+    if (K == 0) return launch_team_batch_one<A, 0>(items, n_items, total_tiles, smem_bytes, grid_cap, tcq, stream);
+    return launch_team_batch_one<A, 4>(items, n_items, total_tiles, smem_bytes, grid_cap, tcq, stream);
 }
 
 }  // namespace pbr

@@ -58,6 +58,32 @@ def test_batch_matches_single_model_runs():
             assert np.isclose(ests[i][key], ref[key], rtol=1e-8), (i, key)
 
 
+def test_batch_tensor_core_groups_match_single_model_runs():
+    """Models with 5-8 surfaces and 16+ modes whose tiles need one block per SM form the
+    tensor-core groups (bead records' quadratic part of V by mma.sync); each matches its own
+    single-model evaluation."""
+    from pibronic_gb300 import constants, synthetic
+    from pibronic_gb300.batch import ModelBatch
+    from pibronic_gb300.plan import DevicePlan, PreparedModels
+    from pibronic_gb300.pimc import evaluate_device
+    preps = []
+    for i, (A, N, P) in enumerate([(7, 18, 24), (8, 16, 20), (6, 20, 128), (7, 9, 24), (3, 17, 40)]):
+        m = synthetic.make_coupled_model(A, N, 2000 + i, sd_quadratic=0.0005)
+        beta = constants.beta(250.0)
+        preps.append(PreparedModels(m, synthetic.diagonal_of(m), P, beta=beta, delta_beta=1e-4 * beta))
+    X = [257, 300, 64, 200, 333]
+    seeds = [21 + i for i in range(5)]
+    mb = ModelBatch(preps, X, seeds)
+    mb.run()
+    torch.cuda.synchronize()
+    assert int(mb.status.item()) == 0
+    for i, prep in enumerate(preps):
+        single = evaluate_device(DevicePlan(prep, precision=32, variant=2), X[i], seed=seeds[i], offset=0)
+        sl = slice(int(mb.seg[i]), int(mb.seg[i + 1]))
+        for k in ("s_rho", "s_g", "s_gp", "s_gm"):
+            assert torch.allclose(mb.out[k][sl], single[k], rtol=2e-4, atol=0), (i, k)
+
+
 def test_batch_graph_replay_matches_direct_run():
     from pibronic_gb300.batch import ModelBatch
     preps = _models(5, 5)
