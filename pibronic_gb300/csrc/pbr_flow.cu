@@ -670,6 +670,228 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_kernel(const Layer
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Training-step layers on the tensor cores (hidden width 128, I <= 64, 2J <= 64): the tile's
+// GEMMs by mma.sync m16n8k16 with BF16 operands, each operand split into BF16 hi and lo parts
+// (16 mantissa bits) and three MMAs per step (hi hi, hi lo, lo hi), FP32 accumulation -- about
+// 1e-5 relative, well inside what the optimiser needs.  The weights sit in shared memory
+// transposed, as BF16 hi and lo pairs along K (the layout of a B fragment); activations stay FP32
+// in shared memory and are split when a fragment is loaded.  8 warps: warp w computes rows
+// 16 (w % 4) .. + 15 and one half of the output columns.
+// ---------------------------------------------------------------------------------------------
+constexpr int kMmaH = 128;
+struct MmaDims {
+    int K1, ldw1, ldw2, Op, ldw3, ldya, ldh;
+    __host__ __device__ MmaDims(int I, int J)
+        : K1((I + 15) / 16 * 16), ldw1((I + 15) / 16 * 8 + 4), ldw2(kMmaH / 2 + 4), Op(64), ldw3(kMmaH / 2 + 4),
+          ldya((I + 15) / 16 * 16 + 8), ldh(kMmaH + 8) {}
+    // 32-bit words: W1^T, W2^T, W3^T hi and lo; biases; the ya and h tiles; row sums; index lists
+    __host__ __device__ int fwd_words(int I, int J) const {
+        return 2 * (kMmaH * ldw1 + kMmaH * ldw2 + Op * ldw3) + 2 * kMmaH + Op + kTileS * (ldya + ldh) +
+               2 * kTileS + ((I + J + 3) / 4) * 4;
+    }
+};
+
+// BF16 pair (x0 low, x1 high) rounded to nearest, and the pair of residuals
+__device__ __forceinline__ void split_bf16x2(float x0, float x1, uint32_t& hi, uint32_t& lo) {
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(hi) : "f"(x1), "f"(x0));
+    const float h0 = __uint_as_float(hi << 16), h1 = __uint_as_float(hi & 0xffff0000u);
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(lo) : "f"(x1 - h1), "f"(x0 - h0));
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// acc[nt] += A (64 x 16 ksteps, FP32 rows of lda) x W (W^T as BF16 pairs: wh / wl [n][ldw]) for
+// this warp's 16 rows and NT n-tiles from column n0 (element (row g / g + 8, columns 2t, 2t + 1))
+template <int NT>
+__device__ __forceinline__ void mma_tile(const float* __restrict__ A, int lda, int ksteps,
+                                         const uint32_t* __restrict__ wh, const uint32_t* __restrict__ wl,
+                                         int ldw, int n0, float (&acc)[NT][4]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const float* a0 = A + (16 * (warp & 3) + g) * lda + 2 * t;
+    for (int kk = 0; kk < ksteps; ++kk) {
+        const float2 x0 = *reinterpret_cast<const float2*>(a0 + 16 * kk);
+        const float2 x1 = *reinterpret_cast<const float2*>(a0 + 8 * lda + 16 * kk);
+        const float2 x2 = *reinterpret_cast<const float2*>(a0 + 16 * kk + 8);
+        const float2 x3 = *reinterpret_cast<const float2*>(a0 + 8 * lda + 16 * kk + 8);
+        uint32_t ah[4], al[4];
+        split_bf16x2(x0.x, x0.y, ah[0], al[0]);
+        split_bf16x2(x1.x, x1.y, ah[1], al[1]);
+        split_bf16x2(x2.x, x2.y, ah[2], al[2]);
+        split_bf16x2(x3.x, x3.y, ah[3], al[3]);
+        uint32_t bh[NT][2], bl[NT][2];
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int o = (n0 + 8 * nt + g) * ldw + 8 * kk + t;
+            bh[nt][0] = wh[o]; bh[nt][1] = wh[o + 4];
+            bl[nt][0] = wl[o]; bl[nt][1] = wl[o + 4];
+        }
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) mma_bf16_16816(acc[nt], ah, bh[nt][0], bh[nt][1]);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) mma_bf16_16816(acc[nt], ah, bl[nt][0], bl[nt][1]);
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) mma_bf16_16816(acc[nt], al, bh[nt][0], bh[nt][1]);
+    }
+}
+
+// B [k][n] (get(k, n); entries outside the matrix zero) as BF16 hi / lo pairs along k in rows n of
+// wh / wl.  kNFast: consecutive threads take consecutive n (get reads a row-major B's rows
+// contiguously), else consecutive k pairs; four pairs per thread per round with their eight loads
+// issued before any conversion (one outstanding load per thread left the staging latency-bound).
+template <bool kNFast, typename Get>
+__device__ __forceinline__ void stage_wt(int nrows, int kpairs, int ldw, uint32_t* wh, uint32_t* wl, Get&& get) {
+    constexpr int U = 4;
+    const int total = nrows * kpairs;
+    for (int b = threadIdx.x; b < total; b += U * blockDim.x) {
+        float v0[U], v1[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = b + u * blockDim.x;
+            const int n = kNFast ? i % nrows : i / kpairs, kp = kNFast ? i / nrows : i % kpairs;
+            v0[u] = i < total ? get(2 * kp, n) : 0.f;
+            v1[u] = i < total ? get(2 * kp + 1, n) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = b + u * blockDim.x;
+            if (i >= total) continue;
+            const int n = kNFast ? i % nrows : i / kpairs, kp = kNFast ? i / nrows : i % kpairs;
+            uint32_t h, l;
+            split_bf16x2(v0[u], v1[u], h, l);
+            wh[n * ldw + kp] = h;
+            wl[n * ldw + kp] = l;
+        }
+    }
+}
+
+// The training direction's forward pass of one layer (dir = -1 with saves) on the tensor cores;
+// same outputs, saves and log-determinant updates as flow_tile_fwd_kernel.
+__global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_mma_kernel(const LayerDev L, int dir, int64_t X,
+                                                                         float* __restrict__ y,
+                                                                         double* __restrict__ logdet,
+                                                                         const SaveDev sv) {
+    extern __shared__ __align__(16) uint32_t msm[];
+    const int I = L.I, J = L.J, D = L.D, H = kMmaH;
+    const MmaDims md(I, J);
+    const int K1 = md.K1, ldya = md.ldya, ldh = md.ldh;
+    uint32_t* w1h = msm;                        // [H][ldw1]
+    uint32_t* w1l = w1h + H * md.ldw1;
+    uint32_t* w2h = w1l + H * md.ldw1;          // [H][ldw2]
+    uint32_t* w2l = w2h + H * md.ldw2;
+    uint32_t* w3h = w2l + H * md.ldw2;          // [Op][ldw3]: row 2j + (0: s_j, 1: t_j)
+    uint32_t* w3l = w3h + md.Op * md.ldw3;
+    float* bb1 = reinterpret_cast<float*>(w3l + md.Op * md.ldw3);
+    float* bb2 = bb1 + H;
+    float* bb3 = bb2 + H;                       // [Op], interleaved like w3
+    float* ya = bb3 + md.Op;                    // [64][ldya]
+    float* hs = ya + kTileS * ldya;             // [64][ldh]: h1, then h2
+    float* rsum = hs + kTileS * ldh;            // [2][64]: the two column halves' sums of s per row
+    int* ia = reinterpret_cast<int*>(rsum + 2 * kTileS);
+    int* ib = ia + I;
+    for (int i = threadIdx.x; i < I + J; i += blockDim.x) ia[i] = i < I ? L.idx_a[i] : L.idx_b[i - I];
+    stage_wt<true>(H, K1 / 2, md.ldw1, w1h, w1l, [&](int k, int n) { return k < I ? L.W1[k * H + n] : 0.f; });
+    stage_wt<true>(H, H / 2, md.ldw2, w2h, w2l, [&](int k, int n) { return L.W2[k * H + n]; });
+    stage_wt<true>(md.Op, H / 2, md.ldw3, w3h, w3l, [&](int k, int c) {
+        const int j = c >> 1;
+        return j < J ? L.W3[k * 2 * J + ((c & 1) ? J + j : j)] : 0.f;
+    });
+    for (int i = threadIdx.x; i < 2 * H; i += blockDim.x) bb1[i] = i < H ? L.b1[i] : L.b2[i - H];
+    for (int i = threadIdx.x; i < md.Op; i += blockDim.x) {
+        const int j = i >> 1;
+        bb3[i] = j < J ? L.b3[(i & 1) ? J + j : j] : 0.f;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int r0 = 16 * (warp & 3) + g;          // this thread's rows r0, r0 + 8
+    const int half = warp >> 2;
+    const int64_t ntiles = (X + kTileS - 1) / kTileS;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t x0 = tile * kTileS;
+        __syncthreads();                         // weights staged / the previous tile's readers are done
+        for (int i = threadIdx.x; i < kTileS * K1; i += blockDim.x) {
+            const int s = i / K1, c = i - s * K1;
+            const int64_t x = x0 + s;
+            const float v = (c < I && x < X) ? y[x * D + ia[c]] : 0.f;
+            ya[s * ldya + c] = v;
+            if (sv.ya && c < I && x < X) sv.ya[x * I + c] = v;
+        }
+        __syncthreads();
+        // ---- h1 = tanh(ya W1 + b1), h2 = tanh(h1 W2 + b2): 64 columns per warp ----
+        for (int layer = 0; layer < 2; ++layer) {
+            const int n0 = 64 * half;
+            const float* bias = layer == 0 ? bb1 : bb2;
+            float acc[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt) {
+                const float b0 = bias[n0 + 8 * nt + 2 * t], b1 = bias[n0 + 8 * nt + 2 * t + 1];
+                acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+            }
+            if (layer == 0) mma_tile<8>(ya, ldya, K1 / 16, w1h, w1l, md.ldw1, n0, acc);
+            else mma_tile<8>(hs, ldh, H / 16, w2h, w2l, md.ldw2, n0, acc);
+            if (layer == 1) __syncthreads();      // every read of h1 is done
+            float* save = layer == 0 ? sv.h1 : sv.h2;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int r = r0 + 8 * hh, c = n0 + 8 * nt + 2 * t;
+                    const float2 h = make_float2(tanhf(acc[nt][2 * hh]), tanhf(acc[nt][2 * hh + 1]));
+                    *reinterpret_cast<float2*>(hs + r * ldh + c) = h;
+                    const int64_t x = x0 + r;
+                    if (save && x < X) *reinterpret_cast<float2*>(save + x * H + c) = h;
+                }
+            __syncthreads();
+        }
+        // ---- head (s, t) = h2 W3 + b3 and the affine coupling: 32 columns (16 pairs) per warp ----
+        {
+            const int n0 = 32 * half;
+            float acc[4][4];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt) {
+                const float b0 = bb3[n0 + 8 * nt + 2 * t], b1 = bb3[n0 + 8 * nt + 2 * t + 1];
+                acc[nt][0] = b0; acc[nt][1] = b1; acc[nt][2] = b0; acc[nt][3] = b1;
+            }
+            mma_tile<4>(hs, ldh, H / 16, w3h, w3l, md.ldw3, n0, acc);
+            float ls[2] = {0.f, 0.f};
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int r = r0 + 8 * hh, j = (n0 + 8 * nt + 2 * t) >> 1;
+                    const int64_t x = x0 + r;
+                    if (j >= J || x >= X) continue;
+                    const float sv_s = kKappa * tanhf(acc[nt][2 * hh] / kKappa);
+                    const float to = acc[nt][2 * hh + 1];
+                    const int bi = ib[j];
+                    const float yb = y[x * D + bi];
+                    const float out = (dir > 0) ? fmaf(yb, __expf(sv_s), to) : (yb - to) * __expf(-sv_s);
+                    y[x * D + bi] = out;
+                    ls[hh] += sv_s;
+                    if (sv.s) { sv.s[x * J + j] = sv_s; sv.yb[x * J + j] = out; }
+                }
+#pragma unroll
+            for (int hh = 0; hh < 2; ++hh) {
+                ls[hh] += __shfl_xor_sync(0xffffffffu, ls[hh], 1);
+                ls[hh] += __shfl_xor_sync(0xffffffffu, ls[hh], 2);
+            }
+            if (t == 0) { rsum[half * kTileS + r0] = ls[0]; rsum[half * kTileS + r0 + 8] = ls[1]; }
+            __syncthreads();
+            if (threadIdx.x < kTileS) {
+                const int64_t x = x0 + threadIdx.x;
+                if (x < X) {
+                    const float s = rsum[threadIdx.x] + rsum[kTileS + threadIdx.x];
+                    logdet[x] += (dir > 0) ? static_cast<double>(s) : -static_cast<double>(s);
+                }
+            }
+        }
+    }
+}
+
 // Back-propagation through one layer of the inverse direction, tiled like the forward pass: the
 // coupling terms elementwise, then gz2 = (g_o W3^T) (1 - h2^2), gz1 = (gz2 W2^T) (1 - h1^2) and
 // dL/dya = gz1 W1^T as shared-memory GEMMs against the transposed weights.
@@ -786,12 +1008,127 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_kernel(const Layer
     }
 }
 
+// Back-propagation through one layer on the tensor cores (the shapes of flow_tile_fwd_mma_kernel):
+// the coupling terms elementwise as in flow_tile_bwd_kernel, then gz2 = (g_o W3^T)(1 - h2^2),
+// gz1 = (gz2 W2^T)(1 - h1^2) and dL/dya = gz1 W1^T by the BF16 hi/lo MMAs of mma_tile.
+struct MmaBwdDims {
+    int ldw3, ldw2, ldw1, ldo, ldh;
+    __host__ __device__ MmaBwdDims() : ldw3(32 + 4), ldw2(kMmaH / 2 + 4), ldw1(kMmaH / 2 + 4), ldo(64 + 8), ldh(kMmaH + 8) {}
+    __host__ __device__ int words(int I, int J) const {
+        return 2 * (kMmaH * ldw3 + kMmaH * ldw2 + 64 * ldw1) + kTileS * (ldo + ldh) + ((I + J + 3) / 4) * 4;
+    }
+};
+
+__global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_mma_kernel(const LayerDev L, int64_t X,
+                                                                         float* __restrict__ gy,
+                                                                         const float* __restrict__ rt,
+                                                                         const SaveDev sv, float* __restrict__ g_o,
+                                                                         float* __restrict__ g_z2,
+                                                                         float* __restrict__ g_z1) {
+    extern __shared__ __align__(16) uint32_t msm[];
+    const int I = L.I, J = L.J, D = L.D, O = 2 * J, H = kMmaH;
+    const MmaBwdDims md;
+    const int ldo = md.ldo, ldh = md.ldh;
+    uint32_t* w3h = msm;                        // B of gz2: [h][j] = (W3[h][j] (s), W3[h][J + j] (t))
+    uint32_t* w3l = w3h + H * md.ldw3;
+    uint32_t* w2h = w3l + H * md.ldw3;          // B of gz1: [h][m pairs] = W2[h][2m], W2[h][2m + 1]
+    uint32_t* w2l = w2h + H * md.ldw2;
+    uint32_t* w1h = w2l + H * md.ldw2;          // B of dya: [a][h pairs] = W1[a][2h], W1[a][2h + 1]
+    uint32_t* w1l = w1h + 64 * md.ldw1;
+    float* go = reinterpret_cast<float*>(w1l + 64 * md.ldw1);   // [64][ldo]: (g_s, g_t) of pair j at 2j, 2j + 1
+    float* gz = go + kTileS * ldo;              // [64][ldh]: gz2, then gz1
+    int* ia = reinterpret_cast<int*>(gz + kTileS * ldh);
+    int* ib = ia + I;
+    for (int i = threadIdx.x; i < I + J; i += blockDim.x) ia[i] = i < I ? L.idx_a[i] : L.idx_b[i - I];
+    // stage_wt(get(k, n)) packs B[k][n] pairs along k into row n
+    stage_wt<false>(H, 32, md.ldw3, w3h, w3l, [&](int k, int n) {
+        const int j = k >> 1;
+        return j < J ? L.W3[n * O + ((k & 1) ? J + j : j)] : 0.f;
+    });
+    stage_wt<false>(H, H / 2, md.ldw2, w2h, w2l, [&](int k, int n) { return L.W2[n * H + k]; });
+    stage_wt<false>(64, H / 2, md.ldw1, w1h, w1l, [&](int k, int n) { return n < I ? L.W1[n * H + k] : 0.f; });
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, g = lane >> 2, t = lane & 3;
+    const int r0 = 16 * (warp & 3) + g;
+    const int half = warp >> 2;
+    const int64_t ntiles = (X + kTileS - 1) / kTileS;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t x0 = tile * kTileS;
+        __syncthreads();
+        // ---- coupling: dL/d(s, t) per pair, dL/dyb' in place ----
+        for (int i = threadIdx.x; i < kTileS * 32; i += blockDim.x) {
+            const int s = i >> 5, j = i & 31;
+            const int64_t x = x0 + s;
+            float gos = 0.f, gt = 0.f;
+            if (j < J && x < X) {
+                const int bi = ib[j];
+                const float sj = sv.s[x * J + j], yb = sv.yb[x * J + j];
+                const float gyb = gy[x * D + bi];
+                const float es = __expf(-sj);
+                gos = (-gyb * yb + rt[x]) * (1.0f - (sj / kKappa) * (sj / kKappa));
+                gt = -gyb * es;
+                gy[x * D + bi] = gyb * es;
+                g_o[x * O + j] = gos;
+                g_o[x * O + J + j] = gt;
+            }
+            go[s * ldo + 2 * j] = gos;
+            go[s * ldo + 2 * j + 1] = gt;
+        }
+        __syncthreads();
+        // ---- gz2, then gz1: 64 columns per warp ----
+        for (int stage = 0; stage < 2; ++stage) {
+            const int n0 = 64 * half;
+            float acc[8][4];
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+            if (stage == 0) mma_tile<8>(go, ldo, 4, w3h, w3l, md.ldw3, n0, acc);
+            else mma_tile<8>(gz, ldh, H / 16, w2h, w2l, md.ldw2, n0, acc);
+            if (stage == 1) __syncthreads();      // every read of gz2 is done
+            const float* hsave = stage == 0 ? sv.h2 : sv.h1;
+            float* gout = stage == 0 ? g_z2 : g_z1;
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int r = r0 + 8 * hh, c = n0 + 8 * nt + 2 * t;
+                    const int64_t x = x0 + r;
+                    const bool ok = x < X;
+                    const float2 h = ok ? *reinterpret_cast<const float2*>(hsave + x * H + c) : make_float2(0.f, 0.f);
+                    const float2 v = make_float2(acc[nt][2 * hh] * (1.f - h.x * h.x), acc[nt][2 * hh + 1] * (1.f - h.y * h.y));
+                    *reinterpret_cast<float2*>(gz + r * ldh + c) = v;
+                    if (ok) *reinterpret_cast<float2*>(gout + x * H + c) = v;
+                }
+            __syncthreads();
+        }
+        // ---- dL/dya = gz1 W1^T, added at the a half: 32 columns per warp ----
+        {
+            const int n0 = 32 * half;
+            float acc[4][4];
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+            mma_tile<4>(gz, ldh, H / 16, w1h, w1l, md.ldw1, n0, acc);
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int r = r0 + 8 * (e >> 1), a = n0 + 8 * nt + 2 * t + (e & 1);
+                    const int64_t x = x0 + r;
+                    if (a < I && x < X) gy[x * D + ia[a]] += acc[nt][e];
+                }
+        }
+    }
+}
+
 // C[M][N] (+)= sum_x A[x][M] B[x][N] (the weight gradients: the batch is the reduction): a block
 // computes a 64 x 64 tile of C over one contiguous split of the batch, 256 threads with 4 x 4
 // outputs each from register-blocked outer products (two 128-bit shared loads per 16 FMAs); the
 // splits' partials are added in split order by gemm_tn_reduce, so the result is deterministic.
 constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
 constexpr int kGemmRowsPerSplit = 256;
+static_assert(kGBK * kGBM == 8 * 256 && kGBM == 64 && kGBN == 64, "gemm_tn_partial's staging: 8 elements per thread");
 
 // TF32 hi and lo parts of x (round to nearest), as the 32-bit patterns mma.sync takes
 __device__ __forceinline__ void split_tf32(float x, uint32_t& hi, uint32_t& lo) {
@@ -832,14 +1169,30 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
     const int64_t x0 = split * chunk, x1 = min(X, x0 + chunk);
-    for (int64_t xb = x0; xb < x1; xb += kGBK) {
-        for (int i = threadIdx.x; i < kGBK * kGBM; i += 256) {
-            const int r = i / kGBM, c = i - r * kGBM;
+    // the next kGBK rows of both operands are loaded into registers while the current ones are
+    // multiplied (8 elements of each per thread: element i = threadIdx.x + 256 u of the 32 x 64
+    // tile), then stored after the barrier
+    float na[8], nb[8];
+    auto fetch = [&](int64_t xb) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = threadIdx.x + 256 * u, r = i >> 6, c = i & 63;
             const int64_t xx = xb + r;
-            sa[r][c] = (xx < x1 && tm + c < M) ? A[xx * M + tm + c] : 0.f;
-            sb[r][c] = (xx < x1 && tn + c < N) ? B[xx * N + tn + c] : 0.f;
+            const bool ok = xx < x1;
+            na[u] = (ok && tm + c < M) ? A[xx * M + tm + c] : 0.f;
+            nb[u] = (ok && tn + c < N) ? B[xx * N + tn + c] : 0.f;
+        }
+    };
+    if (x0 < x1) fetch(x0);
+    for (int64_t xb = x0; xb < x1; xb += kGBK) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = threadIdx.x + 256 * u, r = i >> 6, c = i & 63;
+            sa[r][c] = na[u];
+            sb[r][c] = nb[u];
         }
         __syncthreads();
+        if (xb + kGBK < x1) fetch(xb + kGBK);
         if (colsum) {
 #pragma unroll
             for (int kk = 0; kk < 2; ++kk) {
@@ -896,9 +1249,20 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
 __global__ void gemm_tn_reduce(const float* __restrict__ part, int splits, int M, int N, float beta,
                                float* __restrict__ C, float* __restrict__ colsum) {
     const int MN = M * N, total = colsum ? MN + N : MN;
+    const int64_t stride = MN + N;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        // eight running sums over the splits s = u (mod 8), added in u order at the end: eight
+        // independent loads in flight per thread (one running sum made it a chain of dependent
+        // loads), and still a fixed order
+        float a8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        int s = 0;
+        for (; s + 8 <= splits; s += 8)
+#pragma unroll
+            for (int u = 0; u < 8; ++u) a8[u] += part[static_cast<int64_t>(s + u) * stride + i];
+        for (int u = 0; s + u < splits; ++u) a8[u] += part[static_cast<int64_t>(s + u) * stride + i];
         float acc = 0.f;
-        for (int s = 0; s < splits; ++s) acc += part[static_cast<int64_t>(s) * (MN + N) + i];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += a8[u];
         if (i < MN) C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
         else colsum[i - MN] = acc;
     }
@@ -1082,6 +1446,18 @@ int pbr_flow_layer_forward(const pbr_flow_layer* layer, int32_t direction, int64
         if (!save->ya || !save->h1 || !save->h2 || !save->s || !save->yb) return PBR_ERR_ARG;
         sv = SaveDev{save->ya, save->h1, save->h2, save->s, save->yb};
     }
+    // the training direction with saves: the tensor-core tile kernel where its shapes apply
+    if (save && layer->H == kMmaH && layer->I <= 64 && 2 * layer->J <= 64) {
+        const int mb = static_cast<int>(sizeof(uint32_t)) * MmaDims(layer->I, layer->J).fwd_words(layer->I, layer->J);
+        if (mb <= 227 * 1024) {
+            const int grid = tile_grid(flow_tile_fwd_mma_kernel, mb, X);
+            if (grid >= 1) {
+                flow_tile_fwd_mma_kernel<<<grid, kTileThreads, mb, static_cast<cudaStream_t>(stream)>>>(
+                    to_dev(layer), direction, X, y, logdet, sv);
+                return status();
+            }
+        }
+    }
     const int tb = tile_smem(layer, true);
     if (tb > 0) {
         auto run = [&](auto kern) -> int {
@@ -1118,6 +1494,17 @@ int pbr_flow_layer_backward(const pbr_flow_layer* layer, int64_t X, float* gy, c
     if (!save->h1 || !save->h2 || !save->s || !save->yb) return PBR_ERR_ARG;
     if (X == 0) return PBR_OK;
     const SaveDev sv{save->ya, save->h1, save->h2, save->s, save->yb};
+    if (layer->H == kMmaH && layer->I <= 64 && 2 * layer->J <= 64) {
+        const int mb = static_cast<int>(sizeof(uint32_t)) * MmaBwdDims().words(layer->I, layer->J);
+        if (mb <= 227 * 1024) {
+            const int grid = tile_grid(flow_tile_bwd_mma_kernel, mb, X);
+            if (grid >= 1) {
+                flow_tile_bwd_mma_kernel<<<grid, kTileThreads, mb, static_cast<cudaStream_t>(stream)>>>(
+                    to_dev(layer), X, gy, rt, sv, g_o, g_z2, g_z1);
+                return status();
+            }
+        }
+    }
     const int tb = tile_smem(layer, false);
     if (tb > 0) {
         auto run = [&](auto kern) -> int {
