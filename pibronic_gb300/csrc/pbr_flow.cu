@@ -742,11 +742,11 @@ __device__ __forceinline__ void mma_tile(const float* __restrict__ A, int lda, i
 
 // B [k][n] (get(k, n); entries outside the matrix zero) as BF16 hi / lo pairs along k in rows n of
 // wh / wl.  kNFast: consecutive threads take consecutive n (get reads a row-major B's rows
-// contiguously), else consecutive k pairs; four pairs per thread per round with their eight loads
-// issued before any conversion (one outstanding load per thread left the staging latency-bound).
+// contiguously), else consecutive k pairs; eight pairs per thread per round with their sixteen
+// loads issued before any conversion (the staging is bound by L2 latency, not bandwidth).
 template <bool kNFast, typename Get>
 __device__ __forceinline__ void stage_wt(int nrows, int kpairs, int ldw, uint32_t* wh, uint32_t* wl, Get&& get) {
-    constexpr int U = 4;
+    constexpr int U = 8;
     const int total = nrows * kpairs;
     for (int b = threadIdx.x; b < total; b += U * blockDim.x) {
         float v0[U], v1[U];
@@ -813,12 +813,23 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_mma_kernel(const L
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t x0 = tile * kTileS;
         __syncthreads();                         // weights staged / the previous tile's readers are done
-        for (int i = threadIdx.x; i < kTileS * K1; i += blockDim.x) {
-            const int s = i / K1, c = i - s * K1;
-            const int64_t x = x0 + s;
-            const float v = (c < I && x < X) ? y[x * D + ia[c]] : 0.f;
-            ya[s * ldya + c] = v;
-            if (sv.ya && c < I && x < X) sv.ya[x * I + c] = v;
+        // the a half gathered: eight loads per thread issued before the stores
+        for (int b = threadIdx.x; b < kTileS * K1; b += 8 * blockDim.x) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = b + u * blockDim.x, s = i / K1, c = i - s * K1;
+                const int64_t x = x0 + s;
+                v[u] = (i < kTileS * K1 && c < I && x < X) ? y[x * D + ia[c]] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = b + u * blockDim.x, s = i / K1, c = i - s * K1;
+                if (i >= kTileS * K1) continue;
+                ya[s * ldya + c] = v[u];
+                const int64_t x = x0 + s;
+                if (sv.ya && c < I && x < X) sv.ya[x * I + c] = v[u];
+            }
         }
         __syncthreads();
         // ---- h1 = tanh(ya W1 + b1), h2 = tanh(h1 W2 + b2): 64 columns per warp ----
@@ -858,6 +869,15 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_mma_kernel(const L
             }
             mma_tile<4>(hs, ldh, H / 16, w3h, w3l, md.ldw3, n0, acc);
             float ls[2] = {0.f, 0.f};
+            float ybv[4][2];                          // the b half's inputs, loaded together
+#pragma unroll
+            for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int j = (n0 + 8 * nt + 2 * t) >> 1;
+                    const int64_t x = x0 + r0 + 8 * hh;
+                    ybv[nt][hh] = (j < J && x < X) ? y[x * D + ib[j]] : 0.f;
+                }
 #pragma unroll
             for (int nt = 0; nt < 4; ++nt)
 #pragma unroll
@@ -868,7 +888,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_fwd_mma_kernel(const L
                     const float sv_s = kKappa * tanhf(acc[nt][2 * hh] / kKappa);
                     const float to = acc[nt][2 * hh + 1];
                     const int bi = ib[j];
-                    const float yb = y[x * D + bi];
+                    const float yb = ybv[nt][hh];
                     const float out = (dir > 0) ? fmaf(yb, __expf(sv_s), to) : (yb - to) * __expf(-sv_s);
                     y[x * D + bi] = out;
                     ls[hh] += sv_s;
@@ -1054,25 +1074,38 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_mma_kernel(const L
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t x0 = tile * kTileS;
         __syncthreads();
-        // ---- coupling: dL/d(s, t) per pair, dL/dyb' in place ----
-        for (int i = threadIdx.x; i < kTileS * 32; i += blockDim.x) {
-            const int s = i >> 5, j = i & 31;
-            const int64_t x = x0 + s;
-            float gos = 0.f, gt = 0.f;
-            if (j < J && x < X) {
-                const int bi = ib[j];
-                const float sj = sv.s[x * J + j], yb = sv.yb[x * J + j];
-                const float gyb = gy[x * D + bi];
-                const float es = __expf(-sj);
-                gos = (-gyb * yb + rt[x]) * (1.0f - (sj / kKappa) * (sj / kKappa));
-                gt = -gyb * es;
-                gy[x * D + bi] = gyb * es;
-                g_o[x * O + j] = gos;
-                g_o[x * O + J + j] = gt;
+        // ---- coupling: dL/d(s, t) per pair, dL/dyb' in place (each thread's eight pairs' loads
+        //      issued together) ----
+        {
+            float sj[8], ybv[8], gyb[8], rx[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = threadIdx.x + u * blockDim.x, s = i >> 5, j = i & 31;
+                const int64_t x = x0 + s;
+                const bool ok = j < J && x < X;
+                sj[u] = ok ? sv.s[x * J + j] : 0.f;
+                ybv[u] = ok ? sv.yb[x * J + j] : 0.f;
+                gyb[u] = ok ? gy[x * D + ib[j]] : 0.f;
+                rx[u] = ok ? rt[x] : 0.f;
             }
-            go[s * ldo + 2 * j] = gos;
-            go[s * ldo + 2 * j + 1] = gt;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int i = threadIdx.x + u * blockDim.x, s = i >> 5, j = i & 31;
+                const int64_t x = x0 + s;
+                float gos = 0.f, gt = 0.f;
+                if (j < J && x < X) {
+                    const float es = __expf(-sj[u]);
+                    gos = (-gyb[u] * ybv[u] + rx[u]) * (1.0f - (sj[u] / kKappa) * (sj[u] / kKappa));
+                    gt = -gyb[u] * es;
+                    gy[x * D + ib[j]] = gyb[u] * es;
+                    g_o[x * O + j] = gos;
+                    g_o[x * O + J + j] = gt;
+                }
+                go[s * ldo + 2 * j] = gos;
+                go[s * ldo + 2 * j + 1] = gt;
+            }
         }
+        static_assert(kTileS * 32 == 8 * kTileThreads, "the coupling's eight pairs per thread");
         __syncthreads();
         // ---- gz2, then gz1: 64 columns per warp ----
         for (int stage = 0; stage < 2; ++stage) {
@@ -1087,6 +1120,15 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_mma_kernel(const L
             if (stage == 1) __syncthreads();      // every read of gz2 is done
             const float* hsave = stage == 0 ? sv.h2 : sv.h1;
             float* gout = stage == 0 ? g_z2 : g_z1;
+            float2 hv[8][2];                          // the saved activations, loaded together
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int hh = 0; hh < 2; ++hh) {
+                    const int64_t x = x0 + r0 + 8 * hh;
+                    hv[nt][hh] = x < X ? *reinterpret_cast<const float2*>(hsave + x * H + n0 + 8 * nt + 2 * t)
+                                       : make_float2(0.f, 0.f);
+                }
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)
 #pragma unroll
@@ -1094,7 +1136,7 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_mma_kernel(const L
                     const int r = r0 + 8 * hh, c = n0 + 8 * nt + 2 * t;
                     const int64_t x = x0 + r;
                     const bool ok = x < X;
-                    const float2 h = ok ? *reinterpret_cast<const float2*>(hsave + x * H + c) : make_float2(0.f, 0.f);
+                    const float2 h = hv[nt][hh];
                     const float2 v = make_float2(acc[nt][2 * hh] * (1.f - h.x * h.x), acc[nt][2 * hh + 1] * (1.f - h.y * h.y));
                     *reinterpret_cast<float2*>(gz + r * ldh + c) = v;
                     if (ok) *reinterpret_cast<float2*>(gout + x * H + c) = v;
