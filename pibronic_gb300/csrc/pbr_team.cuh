@@ -49,8 +49,22 @@ __host__ __device__ inline int pow2_ceil(int x) {
     return p;
 }
 
-// bead record: [M: A*A][O series: (K+1)*A][ln S12][M exponent][rho log terms: A] padded to 4
-__host__ __device__ inline int record_len(int A, int K) { return align_up(A * A + (K + 1) * A + 2 + A, 4); }
+// bead record: [M: A*A][O series: (K+1)*A][ln S12][M exponent][rho log terms: A].  From 6
+// surfaces on, M and the O series are each padded to a multiple of 4 so that both sit at 16-byte
+// offsets with whole float4 lengths (128-bit loads in the row teams; no change in length at 6
+// and 8 surfaces).  The record length is an odd multiple of 4 floats: in B1 the 32 threads of a
+// warp write 32 consecutive records, so a length that is a multiple of 32 (the unpadded record at
+// 3 surfaces, 32; at 7, 96) puts every store of the warp in one shared-memory bank, 32-way
+// conflicts, where an odd multiple of 4 gives 4-way (the 7-surface batch group ran 1.4x faster
+// for going from 96 to 100).  Below 6 surfaces M and O stay unpadded: at 5 the padding would grow
+// the record by 13 % and move models out of the two-block build.
+__host__ __device__ constexpr int record_pad(int n, int A) { return A >= 6 ? (n + 3) / 4 * 4 : n; }
+__host__ __device__ constexpr int record_off_o(int A) { return record_pad(A * A, A); }
+__host__ __device__ constexpr int record_off_l(int A, int K) { return record_off_o(A) + record_pad((K + 1) * A, A); }
+__host__ __device__ inline int record_len(int A, int K) {
+    const int n = align_up(record_off_l(A, K) + 2 + A, 4);
+    return (n & 4) ? n : n + 4;
+}
 
 struct TeamPlan {
     int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
@@ -146,7 +160,7 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     constexpr int AP = (A + 3) / 4 * 4;
     constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
     constexpr int TA = (A <= 1) ? 1 : (A <= 2) ? 2 : (A <= 4) ? 4 : 8;
-    constexpr int OFF_O = A * A, OFF_L = A * A + (K + 1) * A, OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
+    constexpr int OFF_O = record_off_o(A), OFF_L = record_off_l(A, K), OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
     constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
     constexpr int NT = kTeamThreads;
     constexpr bool kTwoBlock = MB > 1;
@@ -528,7 +542,7 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
 #pragma unroll
                         for (int c = 0; c < A; ++c) nrow[k][c] = nn[k][c];
                 } else if (r < A) {
-                    T mf[A * A], of[(K + 1) * A];
+                    T mf[OFF_O], of[OFF_L - OFF_O];         // from 6 surfaces whole 128-bit loads
                     ldv(rc_, mf);
                     ldv(rc_ + OFF_O, of);
                     T Mm[A][A], os[K + 1][A];
