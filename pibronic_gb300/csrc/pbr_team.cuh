@@ -161,6 +161,8 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     constexpr int MR = 2 * KP + 2 * AP + 4 + A2P;
     constexpr int TA = (A <= 1) ? 1 : (A <= 2) ? 2 : (A <= 4) ? 4 : 8;
     constexpr int OFF_O = record_off_o(A), OFF_L = record_off_l(A, K), OFF_N = OFF_L + 1, OFF_R = OFF_L + 2;
+    // the O block takes 128-bit stores and loads only at a 16-byte offset
+    static_assert(OFF_O % 4 == 0 || (OFF_L - OFF_O) % 4 != 0, "O block length a multiple of 4 at an unaligned offset");
     constexpr bool kLo = (QM == kQ64) && (sizeof(T) == 4);
     constexpr int NT = kTeamThreads;
     constexpr bool kTwoBlock = MB > 1;
@@ -335,6 +337,9 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                     rec_out[OFF_L] = lmax;
 #pragma unroll
                     for (int a = 0; a < A; ++a) rec_out[OFF_R + a] = (a < nfill) ? phr[a] - lmax : T(0);
+                    T ob[OFF_L - OFF_O];                  // the O series block, row k = order k
+#pragma unroll
+                    for (int i = (K + 1) * A; i < OFF_L - OFF_O; ++i) ob[i] = T(0);
 #pragma unroll
                     for (int a = 0; a < A; ++a) {
                         T ek[K + 1];
@@ -348,8 +353,10 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
                         }
                         const T e0 = dev_exp<T>(phv[0][a] - lmax);
 #pragma unroll
-                        for (int k = 0; k <= K; ++k) rec_out[OFF_O + k * A + a] = e0 * ek[k];
+                        for (int k = 0; k <= K; ++k) ob[k * A + a] = e0 * ek[k];
                     }
+                    // 128-bit stores where the block is float4-aligned (from 6 surfaces on)
+                    stv(rec_out + OFF_O, ob);
                 }
                 if (QM == kQ32V) {
                     const float* vr = args.vq + ((base + s) * static_cast<int64_t>(P) + p) * args.vq_ld;
@@ -437,10 +444,14 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
 #pragma unroll
                     for (int i = 0; i < A2; ++i) vp[i] = v[i];
                     rec_out[OFF_N] = T(expm_neg_tau_packed<A>(vp, static_cast<float>(m.tau), X, f));
+                    T mo[OFF_O];
 #pragma unroll
                     for (int b = 0; b < A; ++b)
 #pragma unroll
-                        for (int c = 0; c < A; ++c) rec_out[b * A + c] = f * X[sym_index(b, c)];
+                        for (int c = 0; c < A; ++c) mo[b * A + c] = f * X[sym_index(b, c)];
+#pragma unroll
+                    for (int i = A * A; i < OFF_O; ++i) mo[i] = T(0);
+                    stv(rec_out, mo);
                 } else {
                     T am[A][A], u[A][A];
 #pragma unroll
