@@ -132,6 +132,36 @@ int check_model(const pbr_model& m, int qmode, const void* q_in, const pbr_outpu
     return PBR_OK;
 }
 
+// Per-sample stride of the register-chunk kernel's q block: N rows of rs floats plus a pad in
+// [1, 32].  A warp holds 32 / G samples x G bead chunks of C beads, and each bead step reads the
+// same mode of all of them (the O series, the linear and the quadratic part of V); the pad is the
+// smallest that spreads those 32 reads over the fewest wavefronts, summed over the chunk's steps
+// (at A = 4, N = 12, P = 64 a pad of 1 put two pairs of lanes in one bank on every read, 2
+// wavefronts, a pad of 2 gives 1).  FP64 keeps a pad of 1.
+int fused_q_stride(int N, int rs, int P, int G, int esz) {
+    const int base = N * rs;
+    if (esz != 4 || G >= 32) return base + 1;
+    const int C = (P + G - 1) / G;
+    int best = base + 1, best_cost = -1;
+    for (int d = 1; d <= 32; ++d) {
+        const int qs = base + d;
+        int cost = 0;
+        for (int ii = 0; ii < C; ++ii) {
+            int cnt[32] = {};
+            int worst = 0;
+            for (int t = 0; t < 32; ++t) {
+                const int p = (t % G) * C + ii;
+                if (p >= P) continue;
+                const int w = (t / G) * qs + p + (p >> 5);
+                worst = std::max(worst, ++cnt[w & 31]);
+            }
+            cost += worst;
+        }
+        if (best_cost < 0 || cost < best_cost) { best_cost = cost; best = qs; }
+    }
+    return best;
+}
+
 int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, uint64_t seed,
               uint64_t offset, const pbr_outputs* out, void* stream) {
     using namespace pbr;
@@ -154,13 +184,13 @@ int run_fused(const pbr_model* model, int qmode, const void* q_in, int64_t X, ui
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
     a.rs = row_stride(m.P);
-    a.qstride = m.N * a.rs + 1;
     // threads per sample: enough that each owns <= kMaxChunk beads, more (up to a warp) when
     // the per-CTA shared memory of S = kThreads / G samples would not fit
     const int esz = m.precision == 32 ? 4 : 8;
     a.G = std::min(32, pow2ceil((m.P + kMaxChunk - 1) / kMaxChunk));
     while (true) {
         a.S = kThreads / a.G;
+        a.qstride = fused_q_stride(m.N, a.rs, m.P, a.G, esz);
         // the tensor-core quadratic where it applies and its tables fit, else the pair loop
         const SmemPlan pt(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride, 1);
         const SmemPlan p0(m.A, m.K, qmode, esz, m.N, m.P, a.S, a.qstride, 0);
