@@ -36,6 +36,20 @@ int ilog2(int x) {
     return l;
 }
 
+// Row stride of the row-team kernel's q block.  For a model that can take the tensor-core
+// quadratic (FP32, 5-8 surfaces, from kTcqMinN modes) the stride is raised to the nearest residue
+// 10, 14, 18 or 22 mod 32: each MMA fragment load reads 8 consecutive beads at the mode offsets of
+// 4 mode quadruples, and those residues spread the 32 reads over the fewest banks for every mode
+// count from 16 to 64 (1.3-1.4 wavefronts per read, against 1.6-2.6 at the residues 2, 4 and 8
+// that row_stride gives at P = 64, 128 and 256).  Residues 2 mod 4 also keep the sampler's
+// per-(sample, mode) chains, which run side by side over consecutive modes, at 2-way conflicts.
+int team_row_stride(const pbr_model& m) {
+    int rs = pbr::row_stride(m.P);
+    if (m.precision != 32 || m.A < 5 || m.A > 8 || m.N < pbr::kTcqMinN) return rs;
+    while (!((rs & 31) == 10 || (rs & 31) == 14 || (rs & 31) == 18 || (rs & 31) == 22)) ++rs;
+    return rs;
+}
+
 // Tile shape of the row-team form for one model: S samples per tile (as many as 256 threads
 // hold, halved until the shared memory fits the budget), G teams per sample, C beads per team.
 int make_team_args(const pbr_model& m, int qmode, const void* q_in, int64_t X, uint64_t seed,
@@ -50,7 +64,7 @@ int make_team_args(const pbr_model& m, int qmode, const void* q_in, int64_t X, u
     a.key0 = static_cast<uint32_t>(seed);
     a.key1 = static_cast<uint32_t>(seed >> 32);
     a.offset = offset;
-    a.rs = row_stride(m.P);
+    a.rs = team_row_stride(m);
     a.qstride = m.N * a.rs + 1;
     a.rl = record_len(m.A, m.K);
     const int esz = m.precision == 32 ? 4 : 8;

@@ -99,9 +99,9 @@ struct TeamPlan {
 };
 
 // Copy one model's tables into the CTA's shared memory (layout TeamPlan; kTcq: the tensor-core
-// quadratic's tables in place of the packed coupling table).
+// quadratic's tables in place of the packed coupling table, its mode offsets in rows of rs).
 template <int A, int K, int QM, typename T, bool kTcq = false>
-__device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan) {
+__device__ void team_load_tables(const pbr_model& m, int rs, T* sm, const TeamPlan& plan) {
     constexpr int A2 = npair(A);
     constexpr int A2P = (A2 + 3) / 4 * 4;
     constexpr int KP = (K + 1 + 3) / 4 * 4;
@@ -122,7 +122,7 @@ __device__ void team_load_tables(const pbr_model& m, T* sm, const TeamPlan& plan
         for (int i = tid; i < (K + 1) * A; i += NT) s_c[i] = g_c[i];
         for (int i = tid; i < A2P; i += NT) s_e[i] = (i < A2) ? g_e[i] : T(0);
         if constexpr (kTcq) {
-            tcq_tables<A>(reinterpret_cast<const float*>(g_qq), N, row_stride(m.P), plan.tcq_k,
+            tcq_tables<A>(reinterpret_cast<const float*>(g_qq), N, rs, plan.tcq_k,
                           reinterpret_cast<uint32_t*>(s_qq));
         } else {
             const int N2 = (QM == kQ32V) ? 0 : npair(N);
@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(kTeamThreads, MB) pimc_team_kernel(const TeamA
     T* sm = reinterpret_cast<T*>(smem_raw);
     const TeamPlan plan(A, K, QM, static_cast<int>(sizeof(T)), args.m.N, args.m.P, args.S, args.G,
                         args.qstride, args.rl, kTcq ? 1 : 0);
-    team_load_tables<A, K, QM, T, kTcq>(args.m, sm, plan);
+    team_load_tables<A, K, QM, T, kTcq>(args.m, args.rs, sm, plan);
     __syncthreads();
     for (int64_t base = static_cast<int64_t>(blockIdx.x) * args.S; base < args.X;
          base += static_cast<int64_t>(gridDim.x) * args.S)
@@ -879,7 +879,7 @@ pimc_team_batch_kernel(const TeamBatchItem* __restrict__ items, int n_items, int
         const TeamArgs& a = items[lo].a;
         if (lo != cur) {
             plan = TeamPlan(A, K, kSample, 4, a.m.N, a.m.P, a.S, a.G, a.qstride, a.rl, kTcq ? 1 : 0);
-            team_load_tables<A, K, kSample, float, kTcq>(a.m, sm, plan);
+            team_load_tables<A, K, kSample, float, kTcq>(a.m, a.rs, sm, plan);
             __syncthreads();
             cur = lo;
         }
