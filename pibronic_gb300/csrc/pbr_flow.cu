@@ -14,6 +14,7 @@
 //   pbr_flow_apply          x = q + sum_s B_s sigma_s (y' - y)
 //   pbr_flow_weights        proposal density of x in the scale of x's PIMC outputs
 //   pbr_adam                Adam update
+#include <algorithm>
 #include <cmath>
 
 #include "pbr_common.cuh"
@@ -1167,9 +1168,13 @@ __global__ void __launch_bounds__(kTileThreads) flow_tile_bwd_mma_kernel(const L
 // C[M][N] (+)= sum_x A[x][M] B[x][N] (the weight gradients: the batch is the reduction): a block
 // computes a 64 x 64 tile of C over one contiguous split of the batch, 256 threads with 4 x 4
 // outputs each from register-blocked outer products (two 128-bit shared loads per 16 FMAs); the
-// splits' partials are added in split order by gemm_tn_reduce, so the result is deterministic.
+// splits' partials are added in a fixed order by gemm_tn_reduce, so the result is deterministic.
 constexpr int kGBM = 64, kGBN = 64, kGBK = 32, kGPad = 4;
-constexpr int kGemmRowsPerSplit = 256;
+// batch rows per split of the weight-gradient GEMM (at most 64 splits); a build-time tunable
+#ifndef PBR_GEMM_ROWS_PER_SPLIT
+#define PBR_GEMM_ROWS_PER_SPLIT 256
+#endif
+constexpr int kGemmRowsPerSplit = PBR_GEMM_ROWS_PER_SPLIT;
 static_assert(kGBK * kGBM == 8 * 256 && kGBM == 64 && kGBN == 64, "gemm_tn_partial's staging: 8 elements per thread");
 
 // TF32 hi and lo parts of x (round to nearest), as the 32-bit patterns mma.sync takes
@@ -1288,25 +1293,34 @@ __global__ void __launch_bounds__(256, 2) gemm_tn_partial(const float* __restric
 }
 
 // partials [splits][M + 1][N] added in split order: rows < M into C, row M into colsum (if any)
-__global__ void gemm_tn_reduce(const float* __restrict__ part, int splits, int M, int N, float beta,
-                               float* __restrict__ C, float* __restrict__ colsum) {
+// C = beta C + the sum of the splits' partial products (and colsum = the sum of their column-sum
+// rows).  A block takes 32 consecutive outputs; its warp u sums the splits s = u (mod 8) in
+// increasing s, and the eight warp sums are added in u order: a fixed order, the same as one
+// thread per output keeping eight running sums, but with 8 loads per thread instead of 64 in
+// sequence (the one-thread form held 16-65 blocks at the training shapes and waited on its loads).
+__global__ void __launch_bounds__(256) gemm_tn_reduce(const float* __restrict__ part, int splits, int M, int N,
+                                                      float beta, float* __restrict__ C, float* __restrict__ colsum) {
+    __shared__ float red[8][32];
     const int MN = M * N, total = colsum ? MN + N : MN;
     const int64_t stride = MN + N;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        // eight running sums over the splits s = u (mod 8), added in u order at the end: eight
-        // independent loads in flight per thread (one running sum made it a chain of dependent
-        // loads), and still a fixed order
-        float a8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        int s = 0;
-        for (; s + 8 <= splits; s += 8)
+    const int lane = threadIdx.x & 31, u = threadIdx.x >> 5;
+    for (int i0 = blockIdx.x * 32; i0 < total; i0 += gridDim.x * 32) {
+        const int i = i0 + lane;
+        float a = 0.f;
+        if (i < total) {
+#pragma unroll 8
+            for (int s = u; s < splits; s += 8) a += part[static_cast<int64_t>(s) * stride + i];
+        }
+        red[u][lane] = a;
+        __syncthreads();
+        if (u == 0 && i < total) {
+            float acc = 0.f;
 #pragma unroll
-            for (int u = 0; u < 8; ++u) a8[u] += part[static_cast<int64_t>(s + u) * stride + i];
-        for (int u = 0; s + u < splits; ++u) a8[u] += part[static_cast<int64_t>(s + u) * stride + i];
-        float acc = 0.f;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) acc += a8[u];
-        if (i < MN) C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
-        else colsum[i - MN] = acc;
+            for (int v = 0; v < 8; ++v) acc += red[v][lane];
+            if (i < MN) C[i] = (beta == 0.f) ? acc : beta * C[i] + acc;   // beta == 0: C may hold garbage
+            else colsum[i - MN] = acc;
+        }
+        __syncthreads();
     }
 }
 
@@ -1591,7 +1605,8 @@ int pbr_gemm_tn_acc(const float* A, const float* B, int64_t X, int32_t M, int32_
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     dim3 grid((M + kGBM - 1) / kGBM, (N + kGBN - 1) / kGBN, static_cast<unsigned>(splits));
     gemm_tn_partial<<<grid, 256, 0, st>>>(A, B, X, M, N, chunk, colsum ? 1 : 0, scratch);
-    gemm_tn_reduce<<<grid_for((static_cast<int64_t>(M) + 1) * N, 256), 256, 0, st>>>(
+    const int64_t outs = (static_cast<int64_t>(M) + 1) * N;
+    gemm_tn_reduce<<<static_cast<int>(std::min<int64_t>((outs + 31) / 32, 8192)), 256, 0, st>>>(
         scratch, static_cast<int>(splits), M, N, beta, C, colsum);
     return status();
 }
