@@ -37,9 +37,10 @@ def _draw(data, X, seed=3):
     return q
 
 
-@pytest.mark.parametrize("N,P,X", [(5, 16, 64), (20, 50, 37), (13, 128, 40)])
+@pytest.mark.parametrize("N,P,X", [(5, 16, 64), (20, 50, 37), (13, 128, 40), (64, 24, 11)])
 def test_prepare_matches_numpy(tmp_path, N, P, X):
-    """P = 50: the scalar bead loop; X not a multiple of the block's whole samples."""
+    """P = 50 and 24: bead counts that are not a multiple of the warp; X not a multiple of the
+    block's whole samples; N = 64: four samples per block."""
     from pibronic_gb300.plan import ring_mode_basis
     FS, data = _box(tmp_path, A=3, N=N, P=P, X=X)
     fl = _flow(data, nsel=3, layers=2, hidden=32)
@@ -58,6 +59,30 @@ def test_prepare_matches_numpy(tmp_path, N, P, X):
     Uref = lam_q.sum(axis=1) - (yref ** 2).sum(axis=(1, 2))
     # FP32 within a mode, FP64 across modes: ~1e-7 relative per mode (a weight moves by e^(dU/2))
     assert np.allclose(U.cpu().numpy(), Uref, rtol=2e-6, atol=1e-6 * N)
+
+
+@pytest.mark.parametrize("N,P,X,nsel", [(5, 16, 64, 3), (20, 50, 37, 3), (13, 128, 41, 2), (7, 33, 9, 5)])
+def test_apply_matches_numpy(tmp_path, N, P, X, nsel):
+    """x = q + sum_s B_s sigma_s (y' - y) against numpy; X N rows not a multiple of the kernel's
+    four-row groups (13 x 41, 7 x 9)."""
+    from pibronic_gb300 import _native
+    from pibronic_gb300.plan import ring_mode_basis
+    FS, data = _box(tmp_path, A=3, N=N, P=P, X=X)
+    fl = _flow(data, nsel=nsel, layers=2, hidden=32)
+    q = _draw(data, X)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    y = torch.randn((X, N * nsel), generator=g, device="cuda")
+    yn = y + 0.1 * torch.randn((X, N * nsel), generator=g, device="cuda")
+    x = torch.empty_like(q)
+    p = _native.ptr
+    _native.check(_native.load().pbr_flow_apply(p(q), p(y), p(yn), X, N, P, nsel, p(fl.t_sigma), p(x),
+                                                _native.stream_handle()), "flow apply")
+    torch.cuda.synchronize()
+    B = ring_mode_basis(P)[:, :nsel]
+    sig = fl.t_sigma.cpu().numpy().reshape(N, nsel)
+    d = (yn - y).double().cpu().numpy().reshape(X, N, nsel) * sig[None]
+    xref = q.double().cpu().numpy() + np.einsum("xjs,ps->xjp", d, B)
+    assert np.allclose(x.double().cpu().numpy(), xref, rtol=1e-6, atol=1e-5)
 
 
 # (N, nsel, layers, hidden, X): sample-tiled layers at hidden 32 / 64 / 128 (ragged last tile, odd
