@@ -783,6 +783,26 @@ def profile_large(args):
     return 0
 
 
+def profile_batched(args):
+    """Profiling helper (no timing, no JSON line): the batched configuration's 256 models, two
+    passes of args.profile_batched samples each, with the kernel form and tile budget the autotuner
+    chose on this part (register chunks up to 4 surfaces, whole-memory row-team tiles from 5), for
+    an ncu capture."""
+    import torch
+    from pibronic_gb300 import synthetic
+    from pibronic_gb300.batch import ModelBatch
+    count, X = args.batch_models, args.profile_batched
+    preps = synthetic.batch_models(count=count, seed=3)
+    mb = ModelBatch(preps, [X] * count, list(range(1, count + 1)),
+                    smem_budget={2: -1, 3: -1, 4: -1, 5: 0, 6: 0, 7: 0, 8: 0})
+    for _ in range(2):
+        mb.run()
+    torch.cuda.synchronize()
+    assert int(mb.status.item()) == 0
+    print("profile-batched done", X, "groups", mb.groups)
+    return 0
+
+
 def profile_learned(args):
     """Profiling helper (no timing, no JSON line): two plain-rho evaluations of args.profile_learned
     samples of the learned-proposal configuration's model (A=6, N=20, P=128, T=200 K, strong
@@ -922,6 +942,8 @@ def main():
                          "configuration's model twice, exit")
     ap.add_argument("--profile-flow", type=int, default=0,
                     help="profiling helper: 20 flow training steps, then this many tensor-core flow samples, exit")
+    ap.add_argument("--profile-batched", type=int, default=0,
+                    help="profiling helper: two passes of the batched models with this many samples each, exit")
     ap.add_argument("--mma-rates", action="store_true",
                     help="profiling helper: sweep the tcgen05 rate probe, print a table, exit")
     args = ap.parse_args()
@@ -933,6 +955,8 @@ def main():
         return profile_large(args)
     if args.profile_learned > 0:
         return profile_learned(args)
+    if args.profile_batched > 0:
+        return profile_batched(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -66,6 +66,17 @@ __host__ __device__ inline int record_len(int A, int K) {
     return (n & 4) ? n : n + 4;
 }
 
+// Combine-slot length: the (K+1) A x A series matrices of a chunk product plus 4, padded so that
+// the slots of the four teams of a warp, each writing its A rows A floats apart, fall in distinct
+// banks (the pad per surface count that gives the fewest store wavefronts for K = 4 and K = 0;
+// unpadded, the 7-surface slots of 249 floats put two teams in the same banks: 4x the wavefronts).
+__host__ __device__ inline int comb_len(int A, int K) {
+    constexpr int pad4[9] = {0, 0, 1, 3, 1, 0, 3, 15, 1};
+    constexpr int pad0[9] = {0, 0, 1, 7, 1, 0, 3, 3, 1};
+    const int a = A < 0 ? 0 : (A > 8 ? 8 : A);
+    return (K + 1) * A * A + 4 + (K > 0 ? pad4[a] : pad0[a]);
+}
+
 struct TeamPlan {
     int c, e, qq, rc, rec, src, q, qlo, beads, lsums, total_bytes;
     int alt;          // second buffer of combine slots (the split combine), or -1: none fits
@@ -85,7 +96,7 @@ struct TeamPlan {
         src = take(S);                                             // ints stored in the slot
         q = take(S * qstride);
         qlo = take((qm == kQ64 && esz == 4) ? S * qstride : 0);
-        const int comb = S * G * ((K + 1) * A * A + 4);
+        const int comb = S * G * comb_len(A, K);
         int nb = S * P * rl;
         nb = nb > comb ? nb : comb;
         beads = take(nb);
@@ -190,7 +201,7 @@ __device__ void team_tile(const TeamArgs& args, T* sm, const TeamPlan& plan, int
     const bool team_ok = team < S * G;
     const int lane = tid & 31;
     const unsigned tmask = (TA == 32) ? 0xffffffffu : (((1u << TA) - 1u) << (lane & ~(TA - 1)));
-    const int CL = (K + 1) * A * A + 4;                    // combine slot length
+    const int CL = comb_len(A, K);                         // combine slot length
 
     {
         const int nvalid = static_cast<int>(min(static_cast<int64_t>(S), args.X - base));
